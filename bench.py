@@ -1,0 +1,393 @@
+"""Benchmark of the CSR SpMM hot path on the GB300.
+
+Workload (default): the power-law SpMM -- A 1,000,000 x 1,000,000, Zipf(1.8)
+row lengths capped at 50,000 with 2 % empty rows, uniform columns, values
+U[-1,1] (seed 0; about 20.6M nonzeros), B dense 1,000,000 x 128 fp32 U[-1,1]
+(seed 1), C 1,000,000 x 128 fp32.  Synthetic stand-in for segTACO's
+SuiteSparse sweep.  Every operand is larger than the 129 MB L2, so no flush is
+needed between steps.
+
+A step is one SpMM C = A B through the C ABI (segtaco_spmm_partition +
+segtaco_spmm), operands resident in HBM.  `value` = algorithmic bytes per
+step / device time per step, where algorithmic bytes = nnz*(4+4) + (M+1)*4 +
+K*N*4 + M*N*4 (index + value streams, row_ptr, B read once, C written once).
+`roofline` is the same byte count over the product kernel's own event-timed
+duration, against the measured HBM copy bandwidth.  `e2e` runs the drop-in
+entry point (segtaco_taco_call, segTACO's spmm_* surface) on pinned host
+operands: copies in, product, copy out, per step.  `cpu_baseline` times the
+oracle's restatement of segTACO's CPU product (Eigen's row-parallel order) on
+this host's cores.
+
+--impl reference runs only that CPU product (the reference arm).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SpMM HBM GB/s (% of roofline)"
+UNIT = "GB/s"
+L2_BYTES = 129e6
+
+
+def algorithmic_bytes(M, K, nnz, N, esz=4):
+    return nnz * 8 + (M + 1) * 4 + K * N * esz + M * N * 4
+
+
+def make_workload(name):
+    from segtaco_gb300 import synth
+    if name == "power_law":
+        A = synth.power_law(seed=0)
+        N = 128
+        desc = "power-law SpMM: A 1Mx1M Zipf(1.8) cap 50000, 2% empty rows, N=128, fp32"
+    elif name == "uniform16":
+        A = synth.uniform_rows(seed=0)
+        N = 32
+        desc = "uniform SpMM: A 16384x16384, 16 nnz/row, N=32, fp32"
+    elif name == "banded":
+        A = synth.banded_plus_random(seed=0)
+        N = 64
+        desc = "banded+random SpMM: A 262144^2, |i-j|<=32 + 8/row, N=64, fp32"
+    else:
+        raise SystemExit("unknown workload " + name)
+    B = synth.dense(A.K, N, seed=1)
+    return A, B, N, desc
+
+
+def peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def committed_traffic(workload, kernel):
+    """Per-launch DRAM bytes of `kernel` on `workload` from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f)[workload][kernel]
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            import tempfile
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def cpu_spmm_timed(A, B, reps, threads=0, frac=1.0):
+    """Time the oracle's FP32 row-parallel product (segTACO's Eigen order) on
+    the first `frac` of the rows; returns (seconds per rep, rows, nnz, threads)."""
+    import numpy as np
+    from oracle import oracle as O
+    M = max(1, int(A.M * frac))
+    rp = np.ascontiguousarray(A.row_ptr[: M + 1])
+    nnz = int(rp[M])
+    col = A.col[:nnz]
+    val = A.val[:nnz]
+    Bc = np.ascontiguousarray(B)
+    out = np.empty((M, B.shape[1]), np.float32)
+    O.cpu_spmm(rp, col, val, Bc, out, threads)  # warm-up (page-in, thread pool)
+    t = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        O.cpu_spmm(rp, col, val, Bc, out, threads)
+        t.append(time.perf_counter() - t0)
+    used = threads if threads > 0 else O.cpu_threads()
+    return statistics.median(t), M, nnz, used
+
+
+def dist_setup(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() and args.impl == "ours" else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def reduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_reference(args, world, rank):
+    """The reference arm: segTACO's CPU product order on this host's cores."""
+    if rank != 0:
+        return
+    A, B, N, desc = make_workload(args.workload)
+    byts = algorithmic_bytes(A.M, A.K, A.nnz, N)
+    # Size each step so warm-up + steps stay within ~2 minutes.
+    t_full, _, _, threads = cpu_spmm_timed(A, B, 1)
+    frac = min(1.0, 120.0 / max(1, args.steps + args.warmup) / max(t_full, 1e-9))
+    frac = max(frac, 0.01)
+    for _ in range(args.warmup):
+        cpu_spmm_timed(A, B, 1, frac=frac)
+    sec, Ms, nnzs, threads = cpu_spmm_timed(A, B, args.steps, frac=frac)
+    share = nnzs / max(1, A.nnz)
+    value = byts * share / sec / 1e9
+    sample = ("rows [0, %d) of the workload (%.1f%% of nonzeros) per step, median of %d steps"
+              % (Ms, 100 * share, args.steps))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(sec * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded numpy PCG64)",
+        "config": {"workload": desc, "M": A.M, "K": A.K, "nnz": A.nnz, "N": N},
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def time_spmm(ops, N_, Ad, Bd, Cd, cfg, ws, stream, steps, warmup):
+    """Per-step device time and product-kernel time (ms) via events on `stream`."""
+    import torch
+    cfg_ready = N_.Config.make(**{**cfg.as_dict(), "flags": cfg.flags | N_.FLAG_PARTITION_READY})
+    for _ in range(warmup):
+        ops.spmm_partition(Ad, Cd, cfg, ws, stream=stream)
+        ops.spmm(Ad, Bd, C_out=Cd, config=cfg_ready, workspace=ws, stream=stream)
+    torch.cuda.synchronize()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+    for i in range(steps):
+        ev[i][0].record(stream)
+        ops.spmm_partition(Ad, Cd, cfg, ws, stream=stream)
+        ev[i][1].record(stream)
+        ops.spmm(Ad, Bd, C_out=Cd, config=cfg_ready, workspace=ws, stream=stream)
+        ev[i][2].record(stream)
+    torch.cuda.synchronize()
+    step = sum(e[0].elapsed_time(e[2]) for e in ev) / steps
+    kern = sum(e[1].elapsed_time(e[2]) for e in ev) / steps
+    return step, kern
+
+
+def run_ours(args, world, rank, local):
+    import numpy as np
+    import torch
+    from segtaco_gb300 import native as N_
+    from segtaco_gb300 import ops, taco
+
+    torch.cuda.set_device(local)
+    A, B, N, desc = make_workload(args.workload)
+    byts = algorithmic_bytes(A.M, A.K, A.nnz, N)
+    Ad = ops.DeviceCSR.from_host(A, "cuda")
+    Bd = torch.from_numpy(B).cuda()
+    Cd = torch.empty((A.M, N), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()
+    peak, peak_kind = peak_hbm()
+
+    if args.schedule == "auto":
+        h = N_.Config()
+        N_.check(N_.lib().segtaco_autotune_heuristic(A.M, A.K, A.nnz, N, N_.F32,
+                                                     int(A.row_lengths().max()), h))
+        cfg = h
+    else:
+        cfg = N_.Config.make(schedule=args.schedule)
+    if args.col_tile:
+        cfg.col_tile = args.col_tile
+    if args.items:
+        cfg.items_per_unit = args.items
+    if args.l2_hints:
+        cfg.flags |= N_.FLAG_L2_HINTS
+    ws_bytes = max(256, ops.spmm_workspace_size(Ad, N, N_.F32, cfg))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+
+    # per-schedule sweep (context for the headline; same workload)
+    schedules = {}
+    if args.all_schedules:
+        for s in ("rb_sr", "rb_pr", "eb_sr", "eb_pr"):
+            c = N_.Config.make(schedule=s, col_tile=cfg.col_tile, flags=cfg.flags)
+            wsz = max(256, ops.spmm_workspace_size(Ad, N, N_.F32, c))
+            w = torch.empty(wsz, dtype=torch.uint8, device="cuda")
+            st, kt = time_spmm(ops, N_, Ad, Bd, Cd, c, w, stream, max(3, args.steps // 2), 2)
+            schedules[s] = {"ms_per_step": round(st, 4), "kernel_ms": round(kt, 4),
+                            "GBps": round(byts / st / 1e6, 1),
+                            "roofline_frac": round(byts / kt / 1e6 / peak, 4)}
+            del w
+
+    sampler = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    sampler.start()
+    step_ms, kern_ms = time_spmm(ops, N_, Ad, Bd, Cd, cfg, ws, stream, args.steps, args.warmup)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    step_ms = reduce_max(step_ms, world)
+    kern_ms = reduce_max(kern_ms, world)
+    value = world * byts / step_ms / 1e6  # GB/s over all ranks
+    achieved = byts / kern_ms / 1e6
+    eb = cfg.schedule in (N_.EB_SR, N_.EB_PR)
+    kernel_name = {N_.RB_SR: "spmm_rb_sr_kernel", N_.RB_PR: "spmm_rb_pr_kernel",
+                   N_.EB_SR: "spmm_eb_sr_kernel", N_.EB_PR: "spmm_eb_pr_kernel"}[cfg.schedule]
+    traffic = committed_traffic(args.workload, kernel_name)
+
+    # e2e through the drop-in surface with pinned host operands
+    e2e = None
+    if not args.no_e2e:
+        name = {N_.RB_SR: "spmm_rb_sr", N_.RB_PR: "spmm_rb_pr", N_.EB_SR: "spmm_eb_sr",
+                N_.EB_PR: "spmm_eb_pr"}[cfg.schedule]
+
+        def pinned(a):
+            t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+            return t, t.numpy()
+        keep = [pinned(x) for x in (A.row_ptr, A.col, A.val, B)]
+        Ch_t = torch.empty((A.M, N), dtype=torch.float32).pin_memory()
+        Ch = Ch_t.numpy()
+        tA, hA = taco.csr(keep[0][1], keep[1][1], keep[2][1], A.M, A.K)
+        tB, hB = taco.dense(keep[3][1])
+        tC, hC = taco.dense(Ch)
+        for _ in range(2):
+            taco.call(name, tC, tA, tB)
+        torch.cuda.synchronize()
+        n_e2e = max(3, min(args.steps, 10))
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(n_e2e):
+            taco.call(name, tC, tA, tB)
+        t_e2e = (time.perf_counter() - t0) / n_e2e
+        t_e2e = reduce_max(t_e2e, world)
+        N_.lib().segtaco_taco_release()
+        h2d = (A.M + 1) * 4 + A.nnz * 8 + A.K * N * 4
+        e2e = {"value": round(world * byts / t_e2e / 1e9, 3), "unit": UNIT,
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": A.M * N * 4,
+               "ms_per_step": round(t_e2e * 1e3, 3), "entry_point": name}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        sec, Ms, nnzs, threads = cpu_spmm_timed(A, B, 2)
+        cpu = {"value": round(byts * (nnzs / A.nnz) / sec / 1e9, 3), "unit": UNIT,
+               "cores": threads, "kind": "port",
+               "sample": "full workload, median of 2 runs after 1 warm-up (%.2f s each)" % sec}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded numpy PCG64)",
+            "config": {"workload": desc, "M": A.M, "K": A.K, "nnz": A.nnz, "N": N,
+                       "schedule": {v: k for k, v in N_.SCHEDULES.items()}[cfg.schedule],
+                       "col_tile": cfg.col_tile, "items_per_unit": cfg.items_per_unit,
+                       "l2_hints": bool(cfg.flags & N_.FLAG_L2_HINTS),
+                       "l2": "no flush: A %.0f MB, B %.0f MB, C %.0f MB each exceed the %.0f MB L2"
+                             % (Ad.nbytes() / 1e6, B.nbytes / 1e6, A.M * N * 4 / 1e6, L2_BYTES / 1e6),
+                       "parallelism": "replicas x%d" % world},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                         "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "traffic": traffic, "kernel": kernel_name,
+                         "kernel_ms": round(kern_ms, 4), "peak_source": peak_kind + " hbm_gbs"},
+            "gpu_launches": args.steps * (2 if eb else 1),
+            "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks, "schedules": schedules,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="power_law", choices=["power_law", "uniform16", "banded"])
+    ap.add_argument("--schedule", default="auto", choices=["auto", "rb_sr", "rb_pr", "eb_sr", "eb_pr"])
+    ap.add_argument("--col-tile", type=int, default=0)
+    ap.add_argument("--items", type=int, default=0)
+    ap.add_argument("--l2-hints", action="store_true")
+    ap.add_argument("--all-schedules", action="store_true", default=True)
+    ap.add_argument("--no-all-schedules", dest="all_schedules", action="store_false")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,384 @@
+// api.cu -- the extern "C" entry points of include/segtaco.h, argument checks,
+// scratch handling and the SpMM planner (schedule / slab width / vector width).
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "internal.h"
+
+namespace segtaco {
+
+static thread_local std::string g_last_error;
+
+int set_error(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int check_cuda(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return SEGTACO_OK;
+  const int code = (e == cudaErrorMemoryAllocation) ? SEGTACO_ENOMEM : SEGTACO_ECUDA;
+  return set_error(code, "%s: %s", what, cudaGetErrorString(e));
+}
+
+int check_launch(const char *what) { return check_cuda(cudaGetLastError(), what); }
+
+Scratch::~Scratch() {
+  if (owned_) cudaFreeAsync(owned_, s_);
+}
+
+int Scratch::reserve(size_t total) {
+  total_ = total;
+  used_ = 0;
+  if (total == 0) return SEGTACO_OK;
+  if (user_) {
+    if (cap_ < total)
+      return set_error(SEGTACO_EINVAL, "workspace too small: %zu bytes given, %zu needed", cap_,
+                       total);
+    if (((uintptr_t)user_) & 255)
+      return set_error(SEGTACO_EINVAL, "workspace must be 256-byte aligned");
+    base_ = static_cast<char *>(user_);
+    return SEGTACO_OK;
+  }
+  SEGTACO_TRY(check_cuda(cudaMallocAsync(&owned_, total, s_), "cudaMallocAsync(workspace)"));
+  base_ = static_cast<char *>(owned_);
+  return SEGTACO_OK;
+}
+
+void *Scratch::take(size_t bytes) {
+  void *p = base_ + used_;
+  used_ += align256(bytes);
+  return p;
+}
+
+// ---------------------------------------------------------------------------
+// SpMM planner
+// ---------------------------------------------------------------------------
+static bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
+
+int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, long long ldc,
+              const void *B, const float *C, const segtaco_config *cfg, SpmmPlan *plan) {
+  segtaco_config c{};
+  c.schedule = SEGTACO_AUTO;
+  if (cfg) c = *cfg;
+  const int esz = b_dtype == SEGTACO_BF16 ? 2 : 4;
+  // Vector width: the widest 16-byte-or-less load that N, the strides and the
+  // base pointers allow, for both the B loads and the C stores.
+  int V = c.vec > 0 ? c.vec : 16 / esz;
+  const int vmax = 16 / esz;
+  if (V > vmax || !is_pow2(V))
+    return set_error(SEGTACO_EINVAL, "vec=%d not in {1,2,4%s}", c.vec, esz == 2 ? ",8" : "");
+  auto fits = [&](int v) {
+    const int vc = v < 4 ? v : 4;  // C is stored in float4 pieces
+    return N % v == 0 && ldb % v == 0 && ((uintptr_t)B % (v * esz)) == 0 && ldc % vc == 0 &&
+           ((uintptr_t)C % (vc * 4)) == 0;
+  };
+  while (V > 1 && !fits(V)) V >>= 1;
+  // Slab width W = G*V columns: a 128-byte row segment by default (32 fp32 /
+  // 64 bf16 columns), never wider than N needs.
+  int W = c.col_tile > 0 ? c.col_tile : 128 / esz;
+  if (W % V != 0) W = ((W + V - 1) / V) * V;
+  int G = W / V;
+  if (G < 1) G = 1;
+  if (G > 32) G = 32;
+  while (!is_pow2(G)) --G;
+  while (G > 1 && (G / 2) * V >= N) G >>= 1;  // no idle half-groups
+  W = G * V;
+  int schedule = c.schedule;
+  // Without row-length statistics the merge path is the safe default: its
+  // work per unit is bounded whatever the row-length skew.
+  if (schedule == SEGTACO_AUTO) schedule = SEGTACO_EB_SR;
+  if (schedule < SEGTACO_RB_SR || schedule > SEGTACO_EB_PR)
+    return set_error(SEGTACO_EINVAL, "unknown schedule %d", schedule);
+  plan->schedule = schedule;
+  plan->V = V;
+  plan->G = G;
+  plan->W = W;
+  plan->slabs = (N + W - 1) / W;
+  plan->l2_hints = (c.flags & SEGTACO_FLAG_L2_HINTS) != 0;
+  plan->rows_per_unit = c.rows_per_unit > 0 ? c.rows_per_unit : 1;
+  plan->items_per_unit = 0;
+  plan->nchunks = 0;
+  plan->workspace = 0;
+  if (schedule == SEGTACO_EB_SR || schedule == SEGTACO_EB_PR) {
+    long long D = c.items_per_unit > 0 ? c.items_per_unit : (schedule == SEGTACO_EB_SR ? 256 : 512);
+    if (D < 1) D = 1;
+    const long long total = (long long)M + nnz;
+    long long nch = (total + D - 1) / D;
+    if (nch < 1) nch = 1;
+    plan->items_per_unit = D;
+    plan->nchunks = nch;
+    plan->workspace = 2 * align256((size_t)(nch + 1) * sizeof(int));
+  }
+  (void)K;
+  return SEGTACO_OK;
+}
+
+int run_spmm_planned(const SpmmPlan &plan, int M, int K, long long nnz, const int *row_ptr,
+                     const int *col, const float *vals, const void *B, int b_dtype, long long ldb,
+                     float *C, long long ldc, int N, int *px, int *py, cudaStream_t s,
+                     bool partition_ready) {
+  if (M == 0 || N == 0) return SEGTACO_OK;
+  SpmmLaunch L;
+  L.schedule = plan.schedule;
+  L.dtype = b_dtype;
+  L.V = plan.V;
+  L.G = plan.G;
+  L.l2_hints = plan.l2_hints;
+  L.M = M;
+  L.K = K;
+  L.N = N;
+  L.nnz = nnz;
+  L.row_ptr = row_ptr;
+  L.col = col;
+  L.val = vals;
+  L.B = B;
+  L.ldb = ldb;
+  L.C = C;
+  L.ldc = ldc;
+  L.part_x = px;
+  L.part_y = py;
+  const bool bf16 = b_dtype == SEGTACO_BF16;
+  switch (plan.schedule) {
+    case SEGTACO_RB_SR:
+      L.units = plan.rows_per_unit;
+      return bf16 ? launch_spmm_rb_sr_bf16(L, s) : launch_spmm_rb_sr_f32(L, s);
+    case SEGTACO_RB_PR:
+      L.units = plan.rows_per_unit;
+      return bf16 ? launch_spmm_rb_pr_bf16(L, s) : launch_spmm_rb_pr_f32(L, s);
+    case SEGTACO_EB_SR:
+    case SEGTACO_EB_PR:
+      if (!partition_ready)
+        SEGTACO_TRY(launch_merge_path(row_ptr, M, nnz, plan.items_per_unit, plan.nchunks, px, py,
+                                      C, ldc, N, s));
+      L.units = plan.nchunks;
+      if (plan.schedule == SEGTACO_EB_SR)
+        return bf16 ? launch_spmm_eb_sr_bf16(L, s) : launch_spmm_eb_sr_f32(L, s);
+      return bf16 ? launch_spmm_eb_pr_bf16(L, s) : launch_spmm_eb_pr_f32(L, s);
+    default:
+      return set_error(SEGTACO_EINVAL, "unknown schedule %d", plan.schedule);
+  }
+}
+
+long long spmv_tile_items();
+long long sddmm_block_nnz();
+
+static int check_csr_args(int M, int K, long long nnz, const int *row_ptr, const int *col) {
+  if (M < 0 || K < 0 || nnz < 0) return set_error(SEGTACO_EINVAL, "negative size");
+  if (nnz > 0x7fffffffLL) return set_error(SEGTACO_EINVAL, "nnz exceeds int32 indices");
+  if (M > 0 && row_ptr == nullptr) return set_error(SEGTACO_EINVAL, "row_ptr is NULL");
+  if (nnz > 0 && col == nullptr) return set_error(SEGTACO_EINVAL, "col is NULL");
+  return SEGTACO_OK;
+}
+
+}  // namespace segtaco
+
+using namespace segtaco;
+
+extern "C" {
+
+const char *segtaco_version(void) { return "segtaco-gb300 0.1 (sm_103a)"; }
+
+const char *segtaco_last_error(void) { return g_last_error.c_str(); }
+
+int segtaco_device_available(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n > 0 ? 1 : 0;
+}
+
+int segtaco_autotune_heuristic(int32_t M, int32_t K, int64_t nnz, int32_t N, int32_t b_dtype,
+                               int64_t max_row_len, segtaco_config *cfg) {
+  if (!cfg) return set_error(SEGTACO_EINVAL, "cfg is NULL");
+  memset(cfg, 0, sizeof(*cfg));
+  const double mean = M > 0 ? (double)nnz / M : 0.0;
+  // Row-balanced sequential when rows are short and even; merge path otherwise.
+  const bool even = max_row_len >= 0 && mean > 0.0 && (double)max_row_len <= 4.0 * mean + 8.0;
+  cfg->schedule = even ? SEGTACO_RB_SR : SEGTACO_EB_SR;
+  const int esz = b_dtype == SEGTACO_BF16 ? 2 : 4;
+  // Whole B fits comfortably in L2: one slab as wide as N (up to 128 columns).
+  const double bbytes = (double)K * N * esz;
+  cfg->col_tile = bbytes <= 48e6 ? (N <= 128 ? N : 128) : 128 / esz;
+  cfg->items_per_unit = 256;
+  cfg->rows_per_unit = 1;
+  cfg->flags = 0;
+  return SEGTACO_OK;
+}
+
+int segtaco_spmm_workspace_size(int32_t M, int32_t K, int64_t nnz, int32_t N, int32_t b_dtype,
+                                const segtaco_config *cfg, size_t *bytes) {
+  if (!bytes) return set_error(SEGTACO_EINVAL, "bytes is NULL");
+  SpmmPlan plan;
+  // Alignment does not change the workspace: plan with aligned stand-ins.
+  SEGTACO_TRY(plan_spmm(M, K, nnz, N, b_dtype, N, N, nullptr, nullptr, cfg, &plan));
+  *bytes = plan.workspace;
+  return SEGTACO_OK;
+}
+
+int segtaco_spmm(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr, const int32_t *col,
+                 const float *vals, const void *B, int32_t b_dtype, int64_t ldb, float *C,
+                 int64_t ldc, int32_t N, const segtaco_config *cfg, void *workspace,
+                 size_t workspace_bytes, void *stream) {
+  SEGTACO_TRY(check_csr_args(M, K, nnz, row_ptr, col));
+  if (N < 0) return set_error(SEGTACO_EINVAL, "negative N");
+  if (b_dtype != SEGTACO_F32 && b_dtype != SEGTACO_BF16)
+    return set_error(SEGTACO_EINVAL, "unknown dense dtype %d", b_dtype);
+  if (M == 0 || N == 0) return SEGTACO_OK;
+  if (C == nullptr) return set_error(SEGTACO_EINVAL, "C is NULL");
+  if (nnz > 0 && B == nullptr) return set_error(SEGTACO_EINVAL, "B is NULL");
+  if (ldb < N || ldc < N) return set_error(SEGTACO_EINVAL, "ldb/ldc smaller than N");
+  SpmmPlan plan;
+  SEGTACO_TRY(plan_spmm(M, K, nnz, N, b_dtype, ldb, ldc, B, C, cfg, &plan));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Scratch scratch(workspace, workspace_bytes, s);
+  SEGTACO_TRY(scratch.reserve(plan.workspace));
+  int *px = nullptr, *py = nullptr;
+  if (plan.workspace) {
+    px = static_cast<int *>(scratch.take((plan.nchunks + 1) * sizeof(int)));
+    py = static_cast<int *>(scratch.take((plan.nchunks + 1) * sizeof(int)));
+  }
+  const bool ready = cfg && (cfg->flags & SEGTACO_FLAG_PARTITION_READY);
+  if (ready && plan.workspace && !workspace)
+    return set_error(SEGTACO_EINVAL, "PARTITION_READY needs the caller's workspace");
+  return run_spmm_planned(plan, M, K, nnz, row_ptr, col, vals, B, b_dtype, ldb, C, ldc, N, px, py,
+                          s, ready);
+}
+
+int segtaco_spmm_partition(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr, float *C,
+                           int64_t ldc, int32_t N, int32_t b_dtype, const segtaco_config *cfg,
+                           void *workspace, size_t workspace_bytes, void *stream) {
+  SEGTACO_TRY(check_csr_args(M, K, nnz, row_ptr, nullptr));
+  if (M == 0 || N == 0) return SEGTACO_OK;
+  if (C == nullptr || ldc < N) return set_error(SEGTACO_EINVAL, "C is NULL or ldc < N");
+  SpmmPlan plan;
+  SEGTACO_TRY(plan_spmm(M, K, nnz, N, b_dtype, N, ldc, nullptr, C, cfg, &plan));
+  if (!plan.workspace) return SEGTACO_OK;
+  if (!workspace) return set_error(SEGTACO_EINVAL, "segtaco_spmm_partition needs a workspace");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Scratch scratch(workspace, workspace_bytes, s);
+  SEGTACO_TRY(scratch.reserve(plan.workspace));
+  int *px = static_cast<int *>(scratch.take((plan.nchunks + 1) * sizeof(int)));
+  int *py = static_cast<int *>(scratch.take((plan.nchunks + 1) * sizeof(int)));
+  return launch_merge_path(row_ptr, M, nnz, plan.items_per_unit, plan.nchunks, px, py, C, ldc, N,
+                           s);
+}
+
+int segtaco_block_starts_taco(int32_t M, int64_t nnz, const int32_t *row_ptr, int32_t P,
+                              int32_t *out, void *stream) {
+  SEGTACO_TRY(check_csr_args(M, 0, nnz, row_ptr, nullptr));
+  if (P <= 0 || out == nullptr) return set_error(SEGTACO_EINVAL, "P must be > 0, out non-NULL");
+  const long long nblk = (nnz + P - 1) / P;
+  return launch_block_starts_taco(row_ptr, M, P, nblk, out, static_cast<cudaStream_t>(stream));
+}
+
+int segtaco_block_starts_canonical(int32_t M, int64_t nnz, const int32_t *row_ptr, int32_t P,
+                                   int32_t *out, void *stream) {
+  SEGTACO_TRY(check_csr_args(M, 0, nnz, row_ptr, nullptr));
+  if (P <= 0 || out == nullptr) return set_error(SEGTACO_EINVAL, "P must be > 0, out non-NULL");
+  const long long nblk = (nnz + P - 1) / P;
+  return launch_block_starts_canonical(row_ptr, M, P, nblk, out,
+                                       static_cast<cudaStream_t>(stream));
+}
+
+int segtaco_merge_path(int32_t M, int64_t nnz, const int32_t *row_ptr, int64_t D, int32_t *out_x,
+                       int32_t *out_y, void *stream) {
+  SEGTACO_TRY(check_csr_args(M, 0, nnz, row_ptr, nullptr));
+  if (D <= 0 || !out_x || !out_y) return set_error(SEGTACO_EINVAL, "D must be > 0, outputs non-NULL");
+  long long nch = ((long long)M + nnz + D - 1) / D;
+  if (nch < 1) nch = 1;
+  return launch_merge_path(row_ptr, M, nnz, D, nch, out_x, out_y, nullptr, 0, 0,
+                           static_cast<cudaStream_t>(stream));
+}
+
+int segtaco_row_ids(int32_t M, int64_t nnz, const int32_t *row_ptr, int32_t *out, void *stream) {
+  SEGTACO_TRY(check_csr_args(M, 0, nnz, row_ptr, nullptr));
+  if (nnz > 0 && out == nullptr) return set_error(SEGTACO_EINVAL, "out is NULL");
+  return launch_row_ids(row_ptr, M, out, static_cast<cudaStream_t>(stream));
+}
+
+int segtaco_csr_validate(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr,
+                         const int32_t *col, void *stream) {
+  SEGTACO_TRY(check_csr_args(M, K, nnz, row_ptr, col));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Scratch scratch(nullptr, 0, s);
+  SEGTACO_TRY(scratch.reserve(256));
+  int *err = static_cast<int *>(scratch.take(2 * sizeof(int)));
+  SEGTACO_TRY(check_cuda(cudaMemsetAsync(err, 0, 2 * sizeof(int), s), "memset"));
+  SEGTACO_TRY(launch_validate(row_ptr, M, K, nnz, col, err, s));
+  int h[2] = {0, 0};
+  SEGTACO_TRY(check_cuda(cudaMemcpyAsync(h, err, sizeof(h), cudaMemcpyDeviceToHost, s), "copy"));
+  SEGTACO_TRY(check_cuda(cudaStreamSynchronize(s), "sync"));
+  static const char *what[] = {"", "row_ptr[0] != 0", "row_ptr[M] != nnz",
+                               "row_ptr decreases at row", "col out of [0, K) at nonzero"};
+  if (h[0] != 0) return set_error(SEGTACO_EINVAL, "malformed CSR: %s %d", what[h[0] & 7], h[1]);
+  return SEGTACO_OK;
+}
+
+int segtaco_spmv_workspace_size(int32_t M, int64_t nnz, size_t *bytes) {
+  if (!bytes) return set_error(SEGTACO_EINVAL, "bytes is NULL");
+  const long long D = spmv_tile_items();
+  long long nch = ((long long)M + nnz + D - 1) / D;
+  if (nch < 1) nch = 1;
+  *bytes = 2 * align256((size_t)(nch + 1) * sizeof(int));
+  return SEGTACO_OK;
+}
+
+int segtaco_spmv(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr, const int32_t *col,
+                 const float *vals, const float *x, float *y, void *workspace,
+                 size_t workspace_bytes, void *stream) {
+  SEGTACO_TRY(check_csr_args(M, K, nnz, row_ptr, col));
+  if (M == 0) return SEGTACO_OK;
+  if (y == nullptr || (nnz > 0 && x == nullptr)) return set_error(SEGTACO_EINVAL, "x/y is NULL");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  size_t ws = 0;
+  segtaco_spmv_workspace_size(M, nnz, &ws);
+  Scratch scratch(workspace, workspace_bytes, s);
+  SEGTACO_TRY(scratch.reserve(ws));
+  const long long D = spmv_tile_items();
+  long long nch = ((long long)M + nnz + D - 1) / D;
+  if (nch < 1) nch = 1;
+  int *px = static_cast<int *>(scratch.take((nch + 1) * sizeof(int)));
+  int *py = static_cast<int *>(scratch.take((nch + 1) * sizeof(int)));
+  return launch_spmv(M, nnz, row_ptr, col, vals, x, y, px, py, D, nch, s);
+}
+
+int segtaco_sddmm(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr, const int32_t *col,
+                  const float *vals, const void *X, const void *Y, int32_t x_dtype, int64_t ldx,
+                  int64_t ldy, int32_t D, float *out, void *stream) {
+  SEGTACO_TRY(check_csr_args(M, K, nnz, row_ptr, col));
+  if (x_dtype != SEGTACO_F32 && x_dtype != SEGTACO_BF16)
+    return set_error(SEGTACO_EINVAL, "unknown dense dtype %d", x_dtype);
+  if (nnz == 0) return SEGTACO_OK;
+  if (D < 0 || ldx < D || ldy < D) return set_error(SEGTACO_EINVAL, "bad D/ldx/ldy");
+  if (!X || !Y || !out) return set_error(SEGTACO_EINVAL, "X/Y/out is NULL");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const long long P = sddmm_block_nnz();
+  const long long nblk = (nnz + P - 1) / P;
+  Scratch scratch(nullptr, 0, s);
+  SEGTACO_TRY(scratch.reserve(align256((size_t)(nblk + 1) * sizeof(int))));
+  int *starts = static_cast<int *>(scratch.take((nblk + 1) * sizeof(int)));
+  return launch_sddmm(M, nnz, row_ptr, col, vals, X, Y, x_dtype, ldx, ldy, D, out, starts, (int)P,
+                      nblk, s);
+}
+
+int segtaco_spmspv(int32_t M, int32_t K, int64_t nnz, const int32_t *col_ptr,
+                   const int32_t *row_idx, const float *vals, int32_t nx, const int32_t *x_idx,
+                   const float *x_vals, float *y, void *stream) {
+  SEGTACO_TRY(check_csr_args(K, M, nnz, col_ptr, row_idx));
+  if (nx < 0) return set_error(SEGTACO_EINVAL, "negative nx");
+  if (M > 0 && y == nullptr) return set_error(SEGTACO_EINVAL, "y is NULL");
+  if (nx > 0 && (!x_idx || !x_vals)) return set_error(SEGTACO_EINVAL, "x is NULL");
+  return launch_spmspv(M, K, col_ptr, row_idx, vals, nx, x_idx, x_vals, y,
+                       static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

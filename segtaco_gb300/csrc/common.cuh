@@ -1,0 +1,224 @@
+// common.cuh -- device helpers shared by the sm_103a kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "segtaco.h"
+
+namespace segtaco {
+
+constexpr int kCta = 256;  // threads per CTA for every streaming kernel
+
+// ---------------------------------------------------------------------------
+// Loads with explicit cache behaviour (PTX ISA "ld" with cache operators).
+// ---------------------------------------------------------------------------
+
+// CSR index / value streams are read once per column slab: cache-streaming.
+__device__ __forceinline__ int ld_stream(const int *p) { return __ldcs(p); }
+__device__ __forceinline__ float ld_stream(const float *p) { return __ldcs(p); }
+
+// L2 policy for the gathered dense rows: keep them (evict_last) so that the
+// slab of B being gathered stays L2-resident while the CSR streams pass by.
+__device__ __forceinline__ uint64_t l2_policy_evict_last() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+
+__device__ __forceinline__ uint64_t l2_policy_evict_normal() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ uint64_t l2_policy(int evict_last) {
+  return evict_last ? l2_policy_evict_last() : l2_policy_evict_normal();
+}
+
+template <bool kHint>
+__device__ __forceinline__ float4 ld_b4(const float *p, uint64_t pol) {
+  float4 r;
+  if (kHint) {
+    asm volatile("ld.global.nc.L2::cache_hint.v4.f32 {%0,%1,%2,%3}, [%4], %5;"
+                 : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+                 : "l"(p), "l"(pol));
+  } else {
+    r = __ldg(reinterpret_cast<const float4 *>(p));
+  }
+  return r;
+}
+template <bool kHint>
+__device__ __forceinline__ float2 ld_b2(const float *p, uint64_t pol) {
+  float2 r;
+  if (kHint) {
+    asm volatile("ld.global.nc.L2::cache_hint.v2.f32 {%0,%1}, [%2], %3;"
+                 : "=f"(r.x), "=f"(r.y)
+                 : "l"(p), "l"(pol));
+  } else {
+    r = __ldg(reinterpret_cast<const float2 *>(p));
+  }
+  return r;
+}
+template <bool kHint>
+__device__ __forceinline__ float ld_b1(const float *p, uint64_t pol) {
+  float r;
+  if (kHint) {
+    asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(r) : "l"(p), "l"(pol));
+  } else {
+    r = __ldg(p);
+  }
+  return r;
+}
+template <bool kHint>
+__device__ __forceinline__ uint4 ld_u4(const uint16_t *p, uint64_t pol) {
+  uint4 r;
+  if (kHint) {
+    asm volatile("ld.global.nc.L2::cache_hint.v4.u32 {%0,%1,%2,%3}, [%4], %5;"
+                 : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+                 : "l"(p), "l"(pol));
+  } else {
+    r = __ldg(reinterpret_cast<const uint4 *>(p));
+  }
+  return r;
+}
+template <bool kHint>
+__device__ __forceinline__ uint2 ld_u2(const uint16_t *p, uint64_t pol) {
+  uint2 r;
+  if (kHint) {
+    asm volatile("ld.global.nc.L2::cache_hint.v2.u32 {%0,%1}, [%2], %3;"
+                 : "=r"(r.x), "=r"(r.y)
+                 : "l"(p), "l"(pol));
+  } else {
+    r = __ldg(reinterpret_cast<const uint2 *>(p));
+  }
+  return r;
+}
+template <bool kHint>
+__device__ __forceinline__ uint32_t ld_u1(const uint16_t *p, uint64_t pol) {
+  uint32_t r;
+  if (kHint) {
+    asm volatile("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(r) : "l"(p), "l"(pol));
+  } else {
+    r = __ldg(reinterpret_cast<const unsigned int *>(p));
+  }
+  return r;
+}
+
+// bf16 bit pattern -> float (exact: bf16 is the top half of a float).
+__device__ __forceinline__ float bf16lo(uint32_t w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float bf16hi(uint32_t w) { return __uint_as_float(w & 0xffff0000u); }
+
+// Load V consecutive dense elements starting at p into float registers.
+// float: V in {1,2,4}; bf16 (uint16_t): V in {1,2,4,8}.
+template <typename BT, int V, bool kHint> struct DenseLoad;
+
+template <bool H> struct DenseLoad<float, 4, H> {
+  static __device__ __forceinline__ void run(const float *p, float (&o)[4], uint64_t pol) {
+    float4 t = ld_b4<H>(p, pol);
+    o[0] = t.x; o[1] = t.y; o[2] = t.z; o[3] = t.w;
+  }
+};
+template <bool H> struct DenseLoad<float, 2, H> {
+  static __device__ __forceinline__ void run(const float *p, float (&o)[2], uint64_t pol) {
+    float2 t = ld_b2<H>(p, pol);
+    o[0] = t.x; o[1] = t.y;
+  }
+};
+template <bool H> struct DenseLoad<float, 1, H> {
+  static __device__ __forceinline__ void run(const float *p, float (&o)[1], uint64_t pol) {
+    o[0] = ld_b1<H>(p, pol);
+  }
+};
+template <bool H> struct DenseLoad<uint16_t, 8, H> {
+  static __device__ __forceinline__ void run(const uint16_t *p, float (&o)[8], uint64_t pol) {
+    uint4 t = ld_u4<H>(p, pol);
+    o[0] = bf16lo(t.x); o[1] = bf16hi(t.x); o[2] = bf16lo(t.y); o[3] = bf16hi(t.y);
+    o[4] = bf16lo(t.z); o[5] = bf16hi(t.z); o[6] = bf16lo(t.w); o[7] = bf16hi(t.w);
+  }
+};
+template <bool H> struct DenseLoad<uint16_t, 4, H> {
+  static __device__ __forceinline__ void run(const uint16_t *p, float (&o)[4], uint64_t pol) {
+    uint2 t = ld_u2<H>(p, pol);
+    o[0] = bf16lo(t.x); o[1] = bf16hi(t.x); o[2] = bf16lo(t.y); o[3] = bf16hi(t.y);
+  }
+};
+template <bool H> struct DenseLoad<uint16_t, 2, H> {
+  static __device__ __forceinline__ void run(const uint16_t *p, float (&o)[2], uint64_t pol) {
+    uint32_t t = ld_u1<H>(p, pol);
+    o[0] = bf16lo(t); o[1] = bf16hi(t);
+  }
+};
+template <bool H> struct DenseLoad<uint16_t, 1, H> {
+  static __device__ __forceinline__ void run(const uint16_t *p, float (&o)[1], uint64_t pol) {
+    (void)pol;
+    unsigned short h = __ldg(reinterpret_cast<const unsigned short *>(p));
+    o[0] = __uint_as_float(((uint32_t)h) << 16);
+  }
+};
+
+// Store V floats (streaming: C is written once and never re-read here).
+template <int V> __device__ __forceinline__ void store_c(float *p, const float (&a)[V]) {
+  if constexpr (V == 8) {
+    __stcs(reinterpret_cast<float4 *>(p), make_float4(a[0], a[1], a[2], a[3]));
+    __stcs(reinterpret_cast<float4 *>(p) + 1, make_float4(a[4], a[5], a[6], a[7]));
+  } else if constexpr (V == 4) {
+    __stcs(reinterpret_cast<float4 *>(p), make_float4(a[0], a[1], a[2], a[3]));
+  } else if constexpr (V == 2) {
+    __stcs(reinterpret_cast<float2 *>(p), make_float2(a[0], a[1]));
+  } else {
+    __stcs(p, a[0]);
+  }
+}
+
+// Vector reduction into global memory (red.global.add.v4.f32, sm_90+).
+__device__ __forceinline__ void red_add4(float *p, float a, float b, float c, float d) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1,%2,%3,%4};" ::"l"(p), "f"(a), "f"(b), "f"(c),
+               "f"(d)
+               : "memory");
+}
+__device__ __forceinline__ void red_add2(float *p, float a, float b) {
+  asm volatile("red.global.add.v2.f32 [%0], {%1,%2};" ::"l"(p), "f"(a), "f"(b) : "memory");
+}
+template <int V> __device__ __forceinline__ void atomic_add_c(float *p, const float (&a)[V]) {
+  if constexpr (V == 8) {
+    red_add4(p, a[0], a[1], a[2], a[3]);
+    red_add4(p + 4, a[4], a[5], a[6], a[7]);
+  } else if constexpr (V == 4) {
+    red_add4(p, a[0], a[1], a[2], a[3]);
+  } else if constexpr (V == 2) {
+    red_add2(p, a[0], a[1]);
+  } else {
+    atomicAdd(p, a[0]);
+  }
+}
+
+// Lanes [g*G, g*G+G) of a warp form lane group g.
+template <int G> __device__ __forceinline__ unsigned group_mask(int lane) {
+  if constexpr (G == 32) {
+    (void)lane;
+    return 0xffffffffu;
+  } else {
+    return ((1u << G) - 1u) << ((lane / G) * G);
+  }
+}
+
+__device__ __forceinline__ int imin(int a, int b) { return a < b ? a : b; }
+
+// Merge-path split of diagonal d over {row ends} U {nonzeros}: x = number of
+// row ends taken; row end x sorts before nonzero y when row_ptr[x+1] <= y.
+__device__ __forceinline__ int merge_path_x(const int *__restrict__ row_ptr, int M, long long nnz,
+                                            long long d) {
+  long long lo = d - nnz;
+  if (lo < 0) lo = 0;
+  long long hi = d < M ? d : M;
+  while (lo < hi) {
+    long long pivot = (lo + hi) >> 1;
+    if ((long long)__ldg(row_ptr + pivot + 1) <= d - pivot - 1)
+      lo = pivot + 1;
+    else
+      hi = pivot;
+  }
+  return (int)lo;
+}
+
+}  // namespace segtaco

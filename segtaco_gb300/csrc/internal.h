@@ -1,0 +1,112 @@
+// internal.h -- host-side plumbing shared by the translation units of libsegtaco.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "segtaco.h"
+
+namespace segtaco {
+
+// Records a message for segtaco_last_error() and returns `code`.
+int set_error(int code, const char *fmt, ...);
+// cudaGetLastError() after a launch -> status (message names the kernel).
+int check_launch(const char *what);
+// A CUDA runtime result -> status.
+int check_cuda(cudaError_t e, const char *what);
+
+#define SEGTACO_TRY(expr)          \
+  do {                             \
+    int _st = (expr);              \
+    if (_st != SEGTACO_OK) return _st; \
+  } while (0)
+
+// Scratch memory for one call: either the caller's buffer or a stream-ordered
+// allocation released at the end of the call.
+class Scratch {
+ public:
+  Scratch(void *user, size_t user_bytes, cudaStream_t s) : user_(user), cap_(user_bytes), s_(s) {}
+  ~Scratch();
+  // Carve `bytes` (256-byte aligned) out of the scratch; allocates when the
+  // caller gave none.  Returns SEGTACO_OK or an error status.
+  int reserve(size_t total_bytes);
+  void *take(size_t bytes);
+
+ private:
+  void *user_;
+  size_t cap_;
+  cudaStream_t s_;
+  void *owned_ = nullptr;
+  char *base_ = nullptr;
+  size_t used_ = 0, total_ = 0;
+};
+
+inline size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
+
+// ---- launchers (partition.cu) ----
+int launch_merge_path(const int *row_ptr, int M, long long nnz, long long D, long long nchunks,
+                      int *px, int *py, float *C, long long ldc, int N, cudaStream_t s);
+int launch_block_starts_taco(const int *row_ptr, int M, int P, long long nblk, int *out,
+                             cudaStream_t s);
+int launch_block_starts_canonical(const int *row_ptr, int M, int P, long long nblk, int *out,
+                                  cudaStream_t s);
+int launch_row_ids(const int *row_ptr, int M, int *out, cudaStream_t s);
+int launch_validate(const int *row_ptr, int M, int K, long long nnz, const int *col, int *err,
+                    cudaStream_t s);
+
+// ---- SpMM kernel launch description (spmm_*.cu) ----
+struct SpmmLaunch {
+  int schedule;  // SEGTACO_RB_SR .. SEGTACO_EB_PR
+  int dtype;     // SEGTACO_F32 / SEGTACO_BF16
+  int V, G;      // vector width (elements) and lanes per group
+  bool l2_hints;
+  int M, K, N;
+  long long nnz;
+  const int *row_ptr, *col;
+  const float *val;
+  const void *B;
+  long long ldb;
+  float *C;
+  long long ldc;
+  const int *part_x, *part_y;  // eb only
+  long long units;             // rb: rows per group (sr) / warp (pr); eb: chunk count
+};
+// One launcher per (schedule, dtype); each switches over (V, G, hints).
+int launch_spmm_rb_sr_f32(const SpmmLaunch &L, cudaStream_t s);
+int launch_spmm_rb_pr_f32(const SpmmLaunch &L, cudaStream_t s);
+int launch_spmm_eb_sr_f32(const SpmmLaunch &L, cudaStream_t s);
+int launch_spmm_eb_pr_f32(const SpmmLaunch &L, cudaStream_t s);
+int launch_spmm_rb_sr_bf16(const SpmmLaunch &L, cudaStream_t s);
+int launch_spmm_rb_pr_bf16(const SpmmLaunch &L, cudaStream_t s);
+int launch_spmm_eb_sr_bf16(const SpmmLaunch &L, cudaStream_t s);
+int launch_spmm_eb_pr_bf16(const SpmmLaunch &L, cudaStream_t s);
+
+// Resolved plan of one SpMM call (api.cu).
+struct SpmmPlan {
+  int schedule, V, G, W, slabs;
+  long long rows_per_unit;   // rb
+  long long items_per_unit;  // eb (merge-path D)
+  long long nchunks;         // eb
+  bool l2_hints;
+  size_t workspace;          // bytes
+};
+int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, long long ldc,
+              const void *B, const float *C, const segtaco_config *cfg, SpmmPlan *plan);
+// Runs a planned SpMM with partition arrays already in `px/py` (eb) or none.
+int run_spmm_planned(const SpmmPlan &plan, int M, int K, long long nnz, const int *row_ptr,
+                     const int *col, const float *vals, const void *B, int b_dtype, long long ldb,
+                     float *C, long long ldc, int N, int *px, int *py, cudaStream_t s,
+                     bool partition_ready = false);
+
+// ---- side ops (spmv.cu, sddmm.cu, spmspv.cu) ----
+int launch_spmv(int M, long long nnz, const int *row_ptr, const int *col, const float *val,
+                const float *x, float *y, int *px, int *py, long long D, long long nchunks,
+                cudaStream_t s);
+int launch_sddmm(int M, long long nnz, const int *row_ptr, const int *col, const float *val,
+                 const void *X, const void *Y, int x_dtype, long long ldx, long long ldy, int D,
+                 float *out, int *starts, int P, long long nblk, cudaStream_t s);
+int launch_spmspv(int M, int K, const int *col_ptr, const int *row_idx, const float *val, int nx,
+                  const int *x_idx, const float *x_vals, float *y, cudaStream_t s);
+
+}  // namespace segtaco

@@ -1,0 +1,156 @@
+// sddmm.cu -- out[p] = vals[p] * <X[i,:], Y[j,:]> for every nonzero p = (i, j).
+//
+// segTACO's SDDMM (sddmm_csr_gpu_taco.h:5-150, CPU reference sddmm_csr_gpu.h:9-50)
+// is element-balanced: nonzero blocks with start rows from
+// taco_binarySearchBeforeBlock.  Here a warp takes a block of kSddmmBlock
+// nonzeros whose start row is the canonical block start; a group of G lanes
+// computes one dot product with V-wide loads of X[i] and Y[j] (one 16-byte load
+// per lane for D = 64 fp32 or D = 64 bf16), reduces it with xor shuffles, and
+// the 32 results of a batch leave in one coalesced store.  X[i] is re-read for
+// every nonzero of row i but stays in L1.
+#include <climits>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace segtaco {
+
+constexpr int kSddmmBlock = 256;  // nonzeros per warp
+
+template <typename XT, int V, int G>
+__global__ void __launch_bounds__(kCta) sddmm_kernel(int M, long long nnz,
+                                                    const int *__restrict__ row_ptr,
+                                                    const int *__restrict__ col,
+                                                    const float *__restrict__ val,
+                                                    const XT *__restrict__ X,
+                                                    const XT *__restrict__ Y, long long ldx,
+                                                    long long ldy, int D, float *__restrict__ out,
+                                                    const int *__restrict__ starts,
+                                                    long long nblk) {
+  constexpr int P = 32 / G;  // nonzeros per step
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int g = lane / G, gl = lane & (G - 1);
+  const long long w = (long long)blockIdx.x * (kCta / 32) + threadIdx.x / 32;
+  if (w >= nblk) return;
+  const long long pb = w * kSddmmBlock;
+  const long long pe = pb + kSddmmBlock < nnz ? pb + kSddmmBlock : nnz;
+  int wb = __ldg(starts + w);  // row of nonzero pb
+  int rw = (wb + lane < M) ? __ldg(row_ptr + wb + 1 + lane) : INT_MAX;
+  for (long long p = pb; p < pe; p += 32) {
+    const int nb = (int)(pe - p < 32 ? pe - p : 32);
+    const int mc = lane < nb ? ld_stream(col + p + lane) : 0;
+    const float mv = lane < nb ? (val ? ld_stream(val + p + lane) : 1.0f) : 0.0f;
+    for (;;) {
+      const int adv = __popc(__ballot_sync(FULL, (long long)rw <= p));
+      if (adv == 0) break;
+      wb += adv;
+      rw = (wb + lane < M) ? __ldg(row_ptr + wb + 1 + lane) : INT_MAX;
+    }
+    const bool covered = (long long)__shfl_sync(FULL, rw, 31) > p + nb - 1;
+    float res = 0.0f;
+    for (int s = 0; s * P < nb; ++s) {
+      const int t = s * P + g;
+      const int j = __shfl_sync(FULL, mc, t & 31);
+      int row = wb;
+      if (covered) {
+#pragma unroll
+        for (int gg = 0; gg < P; ++gg) {
+          const unsigned bal = __ballot_sync(FULL, (long long)rw <= p + s * P + gg);
+          if (g == gg) row = wb + __popc(bal);
+        }
+      } else if (t < nb) {
+        int lo = wb, hi = M - 1;
+        const long long q = p + t;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if ((long long)__ldg(row_ptr + mid) <= q)
+            lo = mid;
+          else
+            hi = mid - 1;
+        }
+        row = lo;
+      }
+      float acc = 0.0f;
+      if (t < nb) {
+        const XT *xr = X + (long long)row * ldx;
+        const XT *yr = Y + (long long)j * ldy;
+        for (int k = gl * V; k < D; k += G * V) {
+          float xa[V], ya[V];
+          DenseLoad<XT, V, false>::run(xr + k, xa, 0);
+          DenseLoad<XT, V, false>::run(yr + k, ya, 0);
+#pragma unroll
+          for (int v = 0; v < V; ++v) acc = fmaf(xa[v], ya[v], acc);
+        }
+      }
+#pragma unroll
+      for (int o = 1; o < G; o <<= 1) acc += __shfl_xor_sync(FULL, acc, o);
+      // Nonzero t of this step was reduced by group t - s*P; lane t keeps it.
+      const float r = __shfl_sync(FULL, acc, ((lane - s * P) & (P - 1)) * G);
+      if (lane / P == s) res = r;
+    }
+    if (lane < nb) out[p + lane] = mv * res;
+  }
+}
+
+#define SEGTACO_SDDMM_CASE(XT, V, G)                                                          \
+  case V * 100 + G:                                                                           \
+    sddmm_kernel<XT, V, G><<<grid, kCta, 0, s>>>(M, nnz, row_ptr, col, val,                   \
+                                                 static_cast<const XT *>(X),                  \
+                                                 static_cast<const XT *>(Y), ldx, ldy, D, out, \
+                                                 starts, nblk);                               \
+    break;
+
+int launch_sddmm(int M, long long nnz, const int *row_ptr, const int *col, const float *val,
+                 const void *X, const void *Y, int x_dtype, long long ldx, long long ldy, int D,
+                 float *out, int *starts, int P, long long nblk, cudaStream_t s) {
+  if (nnz == 0) return SEGTACO_OK;
+  (void)P;
+  SEGTACO_TRY(launch_block_starts_canonical(row_ptr, M, kSddmmBlock, nblk, starts, s));
+  const dim3 grid((unsigned)((nblk + (kCta / 32) - 1) / (kCta / 32)));
+  // Vector width: 16-byte loads when D and the strides allow it.
+  const int esz = x_dtype == SEGTACO_BF16 ? 2 : 4;
+  const uintptr_t al = (uintptr_t)X | (uintptr_t)Y;
+  int V = 16 / esz;
+  while (V > 1 && (D % V != 0 || ldx % V != 0 || ldy % V != 0 || (al % (V * esz)) != 0)) V >>= 1;
+  // Lanes per dot product: enough to cover D in one pass, at most 32.
+  int G = 1;
+  while (G < 32 && G * V < D) G <<= 1;
+  if (x_dtype == SEGTACO_BF16) {
+    switch (V * 100 + G) {
+      SEGTACO_SDDMM_CASE(uint16_t, 8, 1) SEGTACO_SDDMM_CASE(uint16_t, 8, 2)
+      SEGTACO_SDDMM_CASE(uint16_t, 8, 4) SEGTACO_SDDMM_CASE(uint16_t, 8, 8)
+      SEGTACO_SDDMM_CASE(uint16_t, 8, 16) SEGTACO_SDDMM_CASE(uint16_t, 8, 32)
+      SEGTACO_SDDMM_CASE(uint16_t, 4, 1) SEGTACO_SDDMM_CASE(uint16_t, 4, 2)
+      SEGTACO_SDDMM_CASE(uint16_t, 4, 4) SEGTACO_SDDMM_CASE(uint16_t, 4, 8)
+      SEGTACO_SDDMM_CASE(uint16_t, 4, 16) SEGTACO_SDDMM_CASE(uint16_t, 4, 32)
+      SEGTACO_SDDMM_CASE(uint16_t, 2, 1) SEGTACO_SDDMM_CASE(uint16_t, 2, 2)
+      SEGTACO_SDDMM_CASE(uint16_t, 2, 4) SEGTACO_SDDMM_CASE(uint16_t, 2, 8)
+      SEGTACO_SDDMM_CASE(uint16_t, 2, 16) SEGTACO_SDDMM_CASE(uint16_t, 2, 32)
+      SEGTACO_SDDMM_CASE(uint16_t, 1, 1) SEGTACO_SDDMM_CASE(uint16_t, 1, 2)
+      SEGTACO_SDDMM_CASE(uint16_t, 1, 4) SEGTACO_SDDMM_CASE(uint16_t, 1, 8)
+      SEGTACO_SDDMM_CASE(uint16_t, 1, 16) SEGTACO_SDDMM_CASE(uint16_t, 1, 32)
+      default:
+        return set_error(SEGTACO_EUNSUPPORTED, "sddmm: no bf16 variant V=%d G=%d", V, G);
+    }
+  } else {
+    switch (V * 100 + G) {
+      SEGTACO_SDDMM_CASE(float, 4, 1) SEGTACO_SDDMM_CASE(float, 4, 2)
+      SEGTACO_SDDMM_CASE(float, 4, 4) SEGTACO_SDDMM_CASE(float, 4, 8)
+      SEGTACO_SDDMM_CASE(float, 4, 16) SEGTACO_SDDMM_CASE(float, 4, 32)
+      SEGTACO_SDDMM_CASE(float, 2, 1) SEGTACO_SDDMM_CASE(float, 2, 2)
+      SEGTACO_SDDMM_CASE(float, 2, 4) SEGTACO_SDDMM_CASE(float, 2, 8)
+      SEGTACO_SDDMM_CASE(float, 2, 16) SEGTACO_SDDMM_CASE(float, 2, 32)
+      SEGTACO_SDDMM_CASE(float, 1, 1) SEGTACO_SDDMM_CASE(float, 1, 2)
+      SEGTACO_SDDMM_CASE(float, 1, 4) SEGTACO_SDDMM_CASE(float, 1, 8)
+      SEGTACO_SDDMM_CASE(float, 1, 16) SEGTACO_SDDMM_CASE(float, 1, 32)
+      default:
+        return set_error(SEGTACO_EUNSUPPORTED, "sddmm: no f32 variant V=%d G=%d", V, G);
+    }
+  }
+  return check_launch("sddmm_kernel");
+}
+
+long long sddmm_block_nnz() { return kSddmmBlock; }
+
+}  // namespace segtaco

@@ -1,0 +1,504 @@
+// taco_shim.cu -- segTACO's named entry points over taco_tensor_t host operands.
+//
+// Every name of gpu_kernels.cuh:11-93 (plus spmm_rb_sr_256_4 and
+// spmm_eb_sr_256_4, defined at spmm_rb_sr.h:334 / spmm_eb_sr.h:834) maps to a
+// schedule and tuning hints of segtaco_spmm().  A call mirrors the segTACO
+// wrapper contract (e.g. spmm_eb_sr.h:908-928 with copy_to_device_spmm /
+// copy_from_device_spmm / free_tensors_spmm, gpu_library.h:474-612):
+//   allocate device copies, copy A and B host->device, time {partition,
+//   kernel} between two events on the legacy default stream (the GPUTimer of
+//   gpu_library.h:818-857), copy C back into C->vals, free.
+// The two cuSPARSE names call cusparseSpMM(CSR_ALG2) on row-major B and C, as
+// segTACO's comparator does (spmm_csr_gpu_cusparse.h:52-260).
+#include <cuda_runtime.h>
+#include <cusparse.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+
+#include "internal.h"
+#include "segtaco_taco.h"
+
+namespace {
+
+using segtaco::set_error;
+using segtaco::check_cuda;
+
+enum Kind { K_SPMM, K_CUSPARSE, K_SPMV, K_SDDMM, K_SPMSPV };
+
+struct Entry {
+  const char *name;
+  Kind kind;
+  int schedule;  // SEGTACO_* schedule (K_SPMM)
+  int vec;       // dense elements per lane (0 = automatic)
+  int rows;      // rows per unit (rb)
+  int items;     // merge-path items per unit (eb)
+  int col_tile;  // dense columns per slab (0 = automatic)
+};
+
+constexpr int RBSR = SEGTACO_RB_SR, RBPR = SEGTACO_RB_PR, EBSR = SEGTACO_EB_SR,
+              EBPR = SEGTACO_EB_PR;
+
+// segTACO's rb_pr tune family spmm_rb_pr_256_{c}_{g}_{group}: g threads split
+// one row, so here P = g groups share a row (G = 32/g lanes per group, slab
+// W = 128/g fp32 columns); c (i,k) pairs per group -> c rows per warp.
+#define RBPR_TUNE(c, g, grp) {"spmm_rb_pr_256_" #c "_" #g "_" #grp, K_SPMM, RBPR, 4, c, 0, 128 / g},
+// spmm_eb_pr_{Nnz}_{group}: Nnz nonzeros per block -> merge-path chunk of Nnz
+// items per warp; group lanes reduce in parallel -> P = group, W = 128/group.
+#define EBPR_TUNE(n, grp) {"spmm_eb_pr_" #n "_" #grp, K_SPMM, EBPR, 4, 1, n, 128 / grp},
+// spmm_rb_sr_256_{r}_{c}: r rows and c columns per thread.
+#define RBSR_TUNE(r, c) {"spmm_rb_sr_256_" #r "_" #c, K_SPMM, RBSR, c, r, 0, 0},
+// spmm_eb_sr_256_{g}_{c}: g nonzeros per thread group, c columns per thread,
+// 64*g*c nonzeros per block -> 64*g merge-path items per group.
+#define EBSR_TUNE(g, c) {"spmm_eb_sr_256_" #g "_" #c, K_SPMM, EBSR, c, 1, 64 * g, 0},
+
+const Entry kEntries[] = {
+    // gpu_kernels.cuh:11-24
+    {"spmm_csr_gpu_taco", K_SPMM, EBSR, 0, 1, 256, 0},       // K6: eb, 256 nnz/block
+    {"spmm_csr_gpu_warp", K_SPMM, RBSR, 0, 1, 0, 0},         // K4: rb_sr
+    {"spmm_csr_gpu_cusparse", K_CUSPARSE, 0, 0, 0, 0, 0},    // cuSPARSE ALG2
+    {"spmm_csr_gpu_reduction", K_SPMM, RBPR, 0, 1, 0, 0},    // K10: rb_pr
+    {"spmm_csr_pr_eb", K_SPMM, EBPR, 0, 1, 256, 0},          // K13: eb_pr
+    {"spmm_csr_cusparse_row", K_CUSPARSE, 0, 0, 0, 0, 0},    // cuSPARSE ALG2, row-major
+    {"spmm_rb_sr_taco", K_SPMM, RBSR, 0, 1, 0, 0},           // K14
+    {"spmm_rb_sr", K_SPMM, RBSR, 0, 1, 0, 0},                // K15
+    {"spmm_rb_pr_taco", K_SPMM, RBPR, 0, 1, 0, 0},           // K19
+    {"spmm_rb_pr", K_SPMM, RBPR, 0, 1, 0, 0},                // K20
+    {"spmm_eb_sr_taco", K_SPMM, EBSR, 0, 1, 256, 0},         // K23
+    {"spmm_eb_sr", K_SPMM, EBSR, 0, 1, 256, 0},              // K24
+    {"spmm_eb_pr_taco", K_SPMM, EBPR, 0, 1, 256, 0},         // K29
+    {"spmm_eb_pr", K_SPMM, EBPR, 0, 1, 512, 0},              // K30
+    // gpu_kernels.cuh:29-33
+    {"spmm_eb_sr_search", K_SPMM, EBSR, 0, 1, 256, 0},       // K25
+    {"spmm_eb_pr_search", K_SPMM, EBPR, 0, 1, 512, 0},       // K32
+    {"spmm_rb_sr_512_64", K_SPMM, RBSR, 2, 4, 0, 0},         // K16: 4 rows x 2 cols / thread
+    {"spmm_eb_sr_512_64", K_SPMM, EBSR, 0, 1, 256, 0},       // K26
+    {"spmm_rb_pr_256", K_SPMM, RBPR, 0, 1, 0, 0},            // K21
+    // gpu_kernels.cuh:34-63 (K22)
+    RBPR_TUNE(1, 4, 4) RBPR_TUNE(2, 4, 4) RBPR_TUNE(4, 4, 4)
+    RBPR_TUNE(1, 8, 4) RBPR_TUNE(2, 8, 4) RBPR_TUNE(4, 8, 4)
+    RBPR_TUNE(1, 8, 8) RBPR_TUNE(2, 8, 8) RBPR_TUNE(4, 8, 8)
+    RBPR_TUNE(1, 16, 4) RBPR_TUNE(2, 16, 4) RBPR_TUNE(4, 16, 4)
+    RBPR_TUNE(1, 16, 8) RBPR_TUNE(2, 16, 8) RBPR_TUNE(4, 16, 8)
+    RBPR_TUNE(1, 16, 16) RBPR_TUNE(2, 16, 16) RBPR_TUNE(4, 16, 16)
+    RBPR_TUNE(1, 32, 4) RBPR_TUNE(2, 32, 4) RBPR_TUNE(4, 32, 4)
+    RBPR_TUNE(1, 32, 8) RBPR_TUNE(2, 32, 8) RBPR_TUNE(4, 32, 8)
+    RBPR_TUNE(1, 32, 16) RBPR_TUNE(2, 32, 16) RBPR_TUNE(4, 32, 16)
+    RBPR_TUNE(1, 32, 32) RBPR_TUNE(2, 32, 32) RBPR_TUNE(4, 32, 32)
+    // gpu_kernels.cuh:64-75 (K31)
+    EBPR_TUNE(256, 32) EBPR_TUNE(256, 16) EBPR_TUNE(256, 8) EBPR_TUNE(256, 4)
+    EBPR_TUNE(128, 32) EBPR_TUNE(128, 16) EBPR_TUNE(128, 8) EBPR_TUNE(128, 4)
+    EBPR_TUNE(64, 32) EBPR_TUNE(64, 16) EBPR_TUNE(64, 8) EBPR_TUNE(64, 4)
+    // gpu_kernels.cuh:76-84 (K18)
+    RBSR_TUNE(1, 1) RBSR_TUNE(1, 2) RBSR_TUNE(1, 4)
+    RBSR_TUNE(2, 1) RBSR_TUNE(2, 2) RBSR_TUNE(2, 4)
+    RBSR_TUNE(4, 1) RBSR_TUNE(4, 2) RBSR_TUNE(4, 4)
+    // gpu_kernels.cuh:85-93 (K28)
+    EBSR_TUNE(4, 1) EBSR_TUNE(4, 2) EBSR_TUNE(4, 4)
+    EBSR_TUNE(8, 1) EBSR_TUNE(8, 2) EBSR_TUNE(8, 4)
+    EBSR_TUNE(16, 1) EBSR_TUNE(16, 2) EBSR_TUNE(16, 4)
+    // defined, not declared (spmm_rb_sr.h:334, spmm_eb_sr.h:834)
+    {"spmm_rb_sr_256_4", K_SPMM, RBSR, 1, 1, 0, 0},          // K17: 1 column / thread
+    {"spmm_eb_sr_256_4", K_SPMM, EBSR, 1, 1, 1024, 0},       // K27: 1024 nnz / block
+    // side operations (gpu_kernels.cuh:6-8,25-27)
+    {"spmv_csr_gpu_taco", K_SPMV, 0, 0, 0, 0, 0},
+    {"sddmm_csr_gpu_taco", K_SDDMM, 0, 0, 0, 0, 0},
+    {"sddmm_csr_gpu_warp", K_SDDMM, 0, 0, 0, 0, 0},
+    {"spmspv_csr_gpu_taco", K_SPMSPV, 0, 0, 0, 0, 0},
+};
+constexpr int kNumEntries = sizeof(kEntries) / sizeof(kEntries[0]);
+
+float g_timer_ms = -1.0f;
+
+// Device copies of the operands.  segTACO allocates and frees them on every
+// call (gpu_library.h:474-520,604-612); here each operand role keeps a
+// grow-only device buffer for the life of the process (or until
+// segtaco_taco_release), so repeated calls -- a sweep runs every kernel 25
+// times -- pay for cudaMalloc once.  The drop-in surface is single-threaded,
+// like segTACO's; the mutex only keeps concurrent misuse from corrupting it.
+std::mutex g_pool_mu;
+struct PoolSlot {
+  void *ptr = nullptr;
+  size_t cap = 0;
+};
+PoolSlot g_pool[8];
+
+class DeviceCopies {
+ public:
+  DeviceCopies() : lock_(g_pool_mu) {}
+  int alloc(void **p, size_t bytes) {
+    *p = nullptr;
+    if (next_ >= 8) return set_error(SEGTACO_EINVAL, "too many operands");
+    PoolSlot &slot = g_pool[next_++];
+    if (bytes == 0) bytes = 4;
+    if (slot.cap < bytes) {
+      if (slot.ptr) cudaFree(slot.ptr);
+      slot.ptr = nullptr;
+      slot.cap = 0;
+      cudaError_t e = cudaMalloc(&slot.ptr, bytes);
+      if (e != cudaSuccess) return check_cuda(e, "cudaMalloc");
+      slot.cap = bytes;
+    }
+    *p = slot.ptr;
+    return SEGTACO_OK;
+  }
+  int upload(void **p, const void *host, size_t bytes) {
+    SEGTACO_TRY(alloc(p, bytes));
+    if (bytes && host)
+      return check_cuda(cudaMemcpy(*p, host, bytes, cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+    return SEGTACO_OK;
+  }
+
+ private:
+  std::lock_guard<std::mutex> lock_;
+  int next_ = 0;
+};
+
+// Events around the timed region on the legacy default stream.
+class RegionTimer {
+ public:
+  RegionTimer() {
+    cudaEventCreate(&a_);
+    cudaEventCreate(&b_);
+  }
+  ~RegionTimer() {
+    cudaEventDestroy(a_);
+    cudaEventDestroy(b_);
+  }
+  void start() { cudaEventRecord(a_, 0); }
+  int stop() {
+    SEGTACO_TRY(check_cuda(cudaEventRecord(b_, 0), "cudaEventRecord"));
+    SEGTACO_TRY(check_cuda(cudaEventSynchronize(b_), "cudaEventSynchronize"));
+    float ms = -1.0f;
+    SEGTACO_TRY(check_cuda(cudaEventElapsedTime(&ms, a_, b_), "cudaEventElapsedTime"));
+    g_timer_ms = ms;
+    return SEGTACO_OK;
+  }
+
+ private:
+  cudaEvent_t a_, b_;
+};
+
+int need(const taco_tensor_t *t, const char *what, bool csr) {
+  if (!t || !t->dimensions) return set_error(SEGTACO_EINVAL, "%s: NULL tensor or dimensions", what);
+  if (csr && (!t->indices || !t->indices[1] || !t->indices[1][0]))
+    return set_error(SEGTACO_EINVAL, "%s: CSR indices missing (indices[1][0])", what);
+  return SEGTACO_OK;
+}
+
+int run_spmm(const Entry &e, taco_tensor_t *C, taco_tensor_t *A, taco_tensor_t *B) {
+  SEGTACO_TRY(need(C, "C", false));
+  SEGTACO_TRY(need(A, "A", true));
+  SEGTACO_TRY(need(B, "B", false));
+  const int M = C->dimensions[0], N = C->dimensions[1], K = B->dimensions[0];
+  if (A->dimensions[0] != M || B->dimensions[1] != N)
+    return set_error(SEGTACO_EINVAL, "shape mismatch: A %d rows, C %dx%d, B %dx%d",
+                     A->dimensions[0], M, N, K, B->dimensions[1]);
+  const int *rp = A->indices[1][0];
+  const long long nnz = M > 0 ? rp[M] : 0;
+  const int *col = A->indices[1][1];
+  if (nnz > 0 && (!col || !A->vals)) return set_error(SEGTACO_EINVAL, "A: col/vals missing");
+  if (!C->vals || (!B->vals && (size_t)K * N)) return set_error(SEGTACO_EINVAL, "vals missing");
+  DeviceCopies dev;
+  void *d_rp, *d_col, *d_val, *d_B, *d_C;
+  SEGTACO_TRY(dev.upload(&d_rp, rp, (size_t)(M + 1) * 4));
+  SEGTACO_TRY(dev.upload(&d_col, col, (size_t)nnz * 4));
+  SEGTACO_TRY(dev.upload(&d_val, A->vals, (size_t)nnz * 4));
+  SEGTACO_TRY(dev.upload(&d_B, B->vals, (size_t)K * N * 4));
+  SEGTACO_TRY(dev.alloc(&d_C, (size_t)M * N * 4));
+  RegionTimer timer;
+  if (e.kind == K_CUSPARSE) {
+    cusparseHandle_t h = nullptr;
+    cusparseSpMatDescr_t mA = nullptr;
+    cusparseDnMatDescr_t mB = nullptr, mC = nullptr;
+    int st = SEGTACO_OK;
+    const float alpha = 1.0f, beta = 0.0f;
+    size_t bytes = 0;
+    void *work = nullptr;
+#define CS(x)                                                                   \
+  do {                                                                          \
+    cusparseStatus_t _c = (x);                                                  \
+    if (_c != CUSPARSE_STATUS_SUCCESS && st == SEGTACO_OK)                      \
+      st = set_error(SEGTACO_ECUDA, "%s: %s", #x, cusparseGetErrorString(_c)); \
+  } while (0)
+    CS(cusparseCreate(&h));
+    CS(cusparseCreateCsr(&mA, M, K, nnz, d_rp, d_col, d_val, CUSPARSE_INDEX_32I,
+                         CUSPARSE_INDEX_32I, CUSPARSE_INDEX_BASE_ZERO, CUDA_R_32F));
+    CS(cusparseCreateDnMat(&mB, K, N, N, d_B, CUDA_R_32F, CUSPARSE_ORDER_ROW));
+    CS(cusparseCreateDnMat(&mC, M, N, N, d_C, CUDA_R_32F, CUSPARSE_ORDER_ROW));
+    CS(cusparseSpMM_bufferSize(h, CUSPARSE_OPERATION_NON_TRANSPOSE,
+                               CUSPARSE_OPERATION_NON_TRANSPOSE, &alpha, mA, mB, &beta, mC,
+                               CUDA_R_32F, CUSPARSE_SPMM_CSR_ALG2, &bytes));
+    if (st == SEGTACO_OK) st = dev.alloc(&work, bytes);
+    if (st == SEGTACO_OK) {
+      timer.start();
+      CS(cusparseSpMM(h, CUSPARSE_OPERATION_NON_TRANSPOSE, CUSPARSE_OPERATION_NON_TRANSPOSE,
+                      &alpha, mA, mB, &beta, mC, CUDA_R_32F, CUSPARSE_SPMM_CSR_ALG2, work));
+      if (st == SEGTACO_OK) st = timer.stop();
+    }
+    if (mA) cusparseDestroySpMat(mA);
+    if (mB) cusparseDestroyDnMat(mB);
+    if (mC) cusparseDestroyDnMat(mC);
+    if (h) cusparseDestroy(h);
+#undef CS
+    SEGTACO_TRY(st);
+  } else {
+    segtaco_config cfg{};
+    cfg.schedule = e.schedule;
+    cfg.vec = e.vec;
+    cfg.rows_per_unit = e.rows;
+    cfg.items_per_unit = e.items;
+    cfg.col_tile = e.col_tile;
+    size_t ws = 0;
+    SEGTACO_TRY(segtaco_spmm_workspace_size(M, K, nnz, N, SEGTACO_F32, &cfg, &ws));
+    void *d_ws = nullptr;
+    if (ws) SEGTACO_TRY(dev.alloc(&d_ws, ws));
+    timer.start();
+    SEGTACO_TRY(segtaco_spmm(M, K, nnz, (const int *)d_rp, (const int *)d_col,
+                             (const float *)d_val, d_B, SEGTACO_F32, N, (float *)d_C, N, N, &cfg,
+                             d_ws, ws, nullptr));
+    SEGTACO_TRY(timer.stop());
+  }
+  SEGTACO_TRY(check_cuda(cudaMemcpy(C->vals, d_C, (size_t)M * N * 4, cudaMemcpyDeviceToHost),
+                         "cudaMemcpy D2H"));
+  return SEGTACO_OK;
+}
+
+int run_spmv(taco_tensor_t *y, taco_tensor_t *A, taco_tensor_t *x) {
+  SEGTACO_TRY(need(y, "y", false));
+  SEGTACO_TRY(need(A, "A", true));
+  SEGTACO_TRY(need(x, "x", false));
+  const int M = A->dimensions[0], K = x->dimensions[0];
+  if (y->dimensions[0] != M) return set_error(SEGTACO_EINVAL, "y length != rows of A");
+  const int *rp = A->indices[1][0];
+  const long long nnz = rp[M];
+  DeviceCopies dev;
+  void *d_rp, *d_col, *d_val, *d_x, *d_y, *d_ws;
+  SEGTACO_TRY(dev.upload(&d_rp, rp, (size_t)(M + 1) * 4));
+  SEGTACO_TRY(dev.upload(&d_col, A->indices[1][1], (size_t)nnz * 4));
+  SEGTACO_TRY(dev.upload(&d_val, A->vals, (size_t)nnz * 4));
+  SEGTACO_TRY(dev.upload(&d_x, x->vals, (size_t)K * 4));
+  SEGTACO_TRY(dev.alloc(&d_y, (size_t)M * 4));
+  size_t ws = 0;
+  segtaco_spmv_workspace_size(M, nnz, &ws);
+  SEGTACO_TRY(dev.alloc(&d_ws, ws));
+  RegionTimer timer;
+  timer.start();
+  SEGTACO_TRY(segtaco_spmv(M, K, nnz, (const int *)d_rp, (const int *)d_col, (const float *)d_val,
+                           (const float *)d_x, (float *)d_y, d_ws, ws, nullptr));
+  SEGTACO_TRY(timer.stop());
+  return check_cuda(cudaMemcpy(y->vals, d_y, (size_t)M * 4, cudaMemcpyDeviceToHost), "D2H");
+}
+
+// A = B .* (C D^T) sampled at B's pattern (sddmm_csr_gpu_taco(A, B, C, D)).
+int run_sddmm(taco_tensor_t *Aout, taco_tensor_t *B, taco_tensor_t *Cd, taco_tensor_t *Dd) {
+  SEGTACO_TRY(need(Aout, "A", false));
+  SEGTACO_TRY(need(B, "B", true));
+  SEGTACO_TRY(need(Cd, "C", false));
+  SEGTACO_TRY(need(Dd, "D", false));
+  const int M = B->dimensions[0], K = Dd->dimensions[0], D = Cd->dimensions[1];
+  if (Cd->dimensions[0] != M || Dd->dimensions[1] != D)
+    return set_error(SEGTACO_EINVAL, "sddmm: C must be rows(B) x D, D must be K x D");
+  const int *rp = B->indices[1][0];
+  const long long nnz = rp[M];
+  DeviceCopies dev;
+  void *d_rp, *d_col, *d_val, *d_X, *d_Y, *d_out;
+  SEGTACO_TRY(dev.upload(&d_rp, rp, (size_t)(M + 1) * 4));
+  SEGTACO_TRY(dev.upload(&d_col, B->indices[1][1], (size_t)nnz * 4));
+  SEGTACO_TRY(dev.upload(&d_val, B->vals, (size_t)nnz * 4));
+  SEGTACO_TRY(dev.upload(&d_X, Cd->vals, (size_t)M * D * 4));
+  SEGTACO_TRY(dev.upload(&d_Y, Dd->vals, (size_t)K * D * 4));
+  SEGTACO_TRY(dev.alloc(&d_out, (size_t)nnz * 4));
+  RegionTimer timer;
+  timer.start();
+  SEGTACO_TRY(segtaco_sddmm(M, K, nnz, (const int *)d_rp, (const int *)d_col,
+                            (const float *)d_val, d_X, d_Y, SEGTACO_F32, D, D, D, (float *)d_out,
+                            nullptr));
+  SEGTACO_TRY(timer.stop());
+  return check_cuda(cudaMemcpy(Aout->vals, d_out, (size_t)nnz * 4, cudaMemcpyDeviceToHost), "D2H");
+}
+
+// y = A x with A given as the CSR of A^T and x sparse (indices[0][0] = {0, nx},
+// indices[0][1] = coordinates), as segTACO's SpMSpV experiment builds them.
+int run_spmspv(taco_tensor_t *y, taco_tensor_t *At, taco_tensor_t *x) {
+  SEGTACO_TRY(need(y, "y", false));
+  SEGTACO_TRY(need(At, "A", true));
+  if (!x || !x->indices || !x->indices[0] || !x->indices[0][0] || !x->indices[0][1])
+    return set_error(SEGTACO_EINVAL, "x: sparse indices missing");
+  const int Kt = At->dimensions[0];  // columns of A = rows of A^T
+  const int M = y->dimensions[0];
+  const int *cp = At->indices[1][0];
+  const long long nnz = cp[Kt];
+  const int nx = x->indices[0][0][1] - x->indices[0][0][0];
+  const int *xi = x->indices[0][1] + x->indices[0][0][0];
+  const float *xv = x->vals + x->indices[0][0][0];
+  DeviceCopies dev;
+  void *d_cp, *d_ri, *d_val, *d_xi, *d_xv, *d_y;
+  SEGTACO_TRY(dev.upload(&d_cp, cp, (size_t)(Kt + 1) * 4));
+  SEGTACO_TRY(dev.upload(&d_ri, At->indices[1][1], (size_t)nnz * 4));
+  SEGTACO_TRY(dev.upload(&d_val, At->vals, (size_t)nnz * 4));
+  SEGTACO_TRY(dev.upload(&d_xi, xi, (size_t)nx * 4));
+  SEGTACO_TRY(dev.upload(&d_xv, xv, (size_t)nx * 4));
+  SEGTACO_TRY(dev.alloc(&d_y, (size_t)M * 4));
+  RegionTimer timer;
+  timer.start();
+  SEGTACO_TRY(segtaco_spmspv(M, Kt, nnz, (const int *)d_cp, (const int *)d_ri,
+                             (const float *)d_val, nx, (const int *)d_xi, (const float *)d_xv,
+                             (float *)d_y, nullptr));
+  SEGTACO_TRY(timer.stop());
+  return check_cuda(cudaMemcpy(y->vals, d_y, (size_t)M * 4, cudaMemcpyDeviceToHost), "D2H");
+}
+
+const Entry *find(const char *name) {
+  if (!name) return nullptr;
+  for (int i = 0; i < kNumEntries; ++i)
+    if (strcmp(kEntries[i].name, name) == 0) return &kEntries[i];
+  return nullptr;
+}
+
+// segTACO's wrappers stop the process on any CUDA error (gpuErrchk).
+void fail_stop(int status, const char *name) {
+  if (status == SEGTACO_OK) return;
+  fprintf(stderr, "GPUassert: %s: %s\n", name, segtaco_last_error());
+  exit(status < 0 ? -status : status);
+}
+
+}  // namespace
+
+extern "C" {
+
+int segtaco_taco_call(const char *name, taco_tensor_t *out, taco_tensor_t *a, taco_tensor_t *b,
+                      taco_tensor_t *c) {
+  const Entry *e = find(name);
+  if (!e) return set_error(SEGTACO_EINVAL, "unknown kernel name '%s'", name ? name : "(null)");
+  switch (e->kind) {
+    case K_SPMM:
+    case K_CUSPARSE:
+      return run_spmm(*e, out, a, b);
+    case K_SPMV:
+      return run_spmv(out, a, b);
+    case K_SDDMM:
+      return run_sddmm(out, a, b, c);
+    case K_SPMSPV:
+      return run_spmspv(out, a, b);
+  }
+  return set_error(SEGTACO_EINVAL, "bad entry kind");
+}
+
+float segtaco_taco_timer_ms(void) { return g_timer_ms; }
+
+void segtaco_taco_release(void) {
+  std::lock_guard<std::mutex> lock(g_pool_mu);
+  for (PoolSlot &slot : g_pool) {
+    if (slot.ptr) cudaFree(slot.ptr);
+    slot = PoolSlot();
+  }
+}
+int segtaco_taco_num_names(void) { return kNumEntries; }
+const char *segtaco_taco_name(int i) { return (i >= 0 && i < kNumEntries) ? kEntries[i].name : nullptr; }
+
+}  // extern "C"
+
+float get_gpu_timer_result() { return g_timer_ms; }
+
+void spmv_csr_gpu_taco(taco_tensor_t *y, taco_tensor_t *A, taco_tensor_t *x) {
+  fail_stop(segtaco_taco_call("spmv_csr_gpu_taco", y, A, x, nullptr), "spmv_csr_gpu_taco");
+}
+void sddmm_csr_gpu_taco(taco_tensor_t *A, taco_tensor_t *B, taco_tensor_t *C, taco_tensor_t *D) {
+  fail_stop(segtaco_taco_call("sddmm_csr_gpu_taco", A, B, C, D), "sddmm_csr_gpu_taco");
+}
+void sddmm_csr_gpu_warp(taco_tensor_t *A, taco_tensor_t *B, taco_tensor_t *C, taco_tensor_t *D) {
+  fail_stop(segtaco_taco_call("sddmm_csr_gpu_warp", A, B, C, D), "sddmm_csr_gpu_warp");
+}
+void spmspv_csr_gpu_taco(taco_tensor_t *y, taco_tensor_t *A, taco_tensor_t *x) {
+  fail_stop(segtaco_taco_call("spmspv_csr_gpu_taco", y, A, x, nullptr), "spmspv_csr_gpu_taco");
+}
+
+#define SEGTACO_SPMM_DEF(name)                                          \
+  void name(taco_tensor_t *C, taco_tensor_t *A, taco_tensor_t *B) {     \
+    fail_stop(segtaco_taco_call(#name, C, A, B, nullptr), #name);       \
+  }
+SEGTACO_SPMM_DEF(spmm_csr_gpu_taco)
+SEGTACO_SPMM_DEF(spmm_csr_gpu_warp)
+SEGTACO_SPMM_DEF(spmm_csr_gpu_cusparse)
+SEGTACO_SPMM_DEF(spmm_csr_gpu_reduction)
+SEGTACO_SPMM_DEF(spmm_csr_pr_eb)
+SEGTACO_SPMM_DEF(spmm_csr_cusparse_row)
+SEGTACO_SPMM_DEF(spmm_rb_sr_taco)
+SEGTACO_SPMM_DEF(spmm_rb_sr)
+SEGTACO_SPMM_DEF(spmm_rb_pr_taco)
+SEGTACO_SPMM_DEF(spmm_rb_pr)
+SEGTACO_SPMM_DEF(spmm_eb_sr_taco)
+SEGTACO_SPMM_DEF(spmm_eb_sr)
+SEGTACO_SPMM_DEF(spmm_eb_pr_taco)
+SEGTACO_SPMM_DEF(spmm_eb_pr)
+SEGTACO_SPMM_DEF(spmm_eb_sr_search)
+SEGTACO_SPMM_DEF(spmm_eb_pr_search)
+SEGTACO_SPMM_DEF(spmm_rb_sr_512_64)
+SEGTACO_SPMM_DEF(spmm_eb_sr_512_64)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_1_4_4)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_2_4_4)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_4_4_4)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_1_8_4)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_2_8_4)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_4_8_4)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_1_8_8)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_2_8_8)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_4_8_8)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_1_16_4)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_2_16_4)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_4_16_4)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_1_16_8)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_2_16_8)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_4_16_8)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_1_16_16)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_2_16_16)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_4_16_16)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_1_32_4)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_2_32_4)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_4_32_4)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_1_32_8)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_2_32_8)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_4_32_8)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_1_32_16)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_2_32_16)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_4_32_16)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_1_32_32)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_2_32_32)
+SEGTACO_SPMM_DEF(spmm_rb_pr_256_4_32_32)
+SEGTACO_SPMM_DEF(spmm_eb_pr_256_32)
+SEGTACO_SPMM_DEF(spmm_eb_pr_256_16)
+SEGTACO_SPMM_DEF(spmm_eb_pr_256_8)
+SEGTACO_SPMM_DEF(spmm_eb_pr_256_4)
+SEGTACO_SPMM_DEF(spmm_eb_pr_128_32)
+SEGTACO_SPMM_DEF(spmm_eb_pr_128_16)
+SEGTACO_SPMM_DEF(spmm_eb_pr_128_8)
+SEGTACO_SPMM_DEF(spmm_eb_pr_128_4)
+SEGTACO_SPMM_DEF(spmm_eb_pr_64_32)
+SEGTACO_SPMM_DEF(spmm_eb_pr_64_16)
+SEGTACO_SPMM_DEF(spmm_eb_pr_64_8)
+SEGTACO_SPMM_DEF(spmm_eb_pr_64_4)
+SEGTACO_SPMM_DEF(spmm_rb_sr_256_1_1)
+SEGTACO_SPMM_DEF(spmm_rb_sr_256_1_2)
+SEGTACO_SPMM_DEF(spmm_rb_sr_256_1_4)
+SEGTACO_SPMM_DEF(spmm_rb_sr_256_2_1)
+SEGTACO_SPMM_DEF(spmm_rb_sr_256_2_2)
+SEGTACO_SPMM_DEF(spmm_rb_sr_256_2_4)
+SEGTACO_SPMM_DEF(spmm_rb_sr_256_4_1)
+SEGTACO_SPMM_DEF(spmm_rb_sr_256_4_2)
+SEGTACO_SPMM_DEF(spmm_rb_sr_256_4_4)
+SEGTACO_SPMM_DEF(spmm_eb_sr_256_4_1)
+SEGTACO_SPMM_DEF(spmm_eb_sr_256_4_2)
+SEGTACO_SPMM_DEF(spmm_eb_sr_256_4_4)
+SEGTACO_SPMM_DEF(spmm_eb_sr_256_8_1)
+SEGTACO_SPMM_DEF(spmm_eb_sr_256_8_2)
+SEGTACO_SPMM_DEF(spmm_eb_sr_256_8_4)
+SEGTACO_SPMM_DEF(spmm_eb_sr_256_16_1)
+SEGTACO_SPMM_DEF(spmm_eb_sr_256_16_2)
+SEGTACO_SPMM_DEF(spmm_eb_sr_256_16_4)
+SEGTACO_SPMM_DEF(spmm_rb_sr_256_4)
+SEGTACO_SPMM_DEF(spmm_eb_sr_256_4)
+#undef SEGTACO_SPMM_DEF

@@ -1,0 +1,137 @@
+"""ctypes bindings of libsegtaco.so (include/segtaco.h, include/segtaco_taco.h).
+
+The library is the product: every compute call below goes through its C ABI.
+There is no fallback -- if the shared library is missing or no CUDA device is
+present, the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsegtaco.so")
+
+OK = 0
+EINVAL = -1
+ECUDA = -2
+ENOMEM = -3
+ETIMEOUT = -4
+EUNSUPPORTED = -5
+ECANCELLED = -6
+EBUSY = -7
+
+AUTO = -1
+RB_SR = 0
+RB_PR = 1
+EB_SR = 2
+EB_PR = 3
+SCHEDULES = {"rb_sr": RB_SR, "rb_pr": RB_PR, "eb_sr": EB_SR, "eb_pr": EB_PR}
+
+F32 = 0
+BF16 = 1
+
+FLAG_L2_HINTS = 1
+FLAG_PARTITION_READY = 2
+
+
+class SegtacoError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__("segtaco error %d: %s" % (code, message))
+        self.code = code
+
+
+class Config(C.Structure):
+    """segtaco_config: zero fields mean automatic."""
+    _fields_ = [("schedule", C.c_int32), ("col_tile", C.c_int32), ("vec", C.c_int32),
+                ("rows_per_unit", C.c_int32), ("items_per_unit", C.c_int32),
+                ("flags", C.c_uint32)]
+
+    @classmethod
+    def make(cls, schedule=AUTO, col_tile=0, vec=0, rows_per_unit=0, items_per_unit=0,
+             flags=0):
+        if isinstance(schedule, str):
+            schedule = SCHEDULES[schedule]
+        return cls(schedule, col_tile, vec, rows_per_unit, items_per_unit, flags)
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class TacoTensor(C.Structure):
+    """taco_tensor_t (segTACO taco_tensor_t.h:6-15), same layout."""
+    _fields_ = [("order", C.c_int32), ("dimensions", C.POINTER(C.c_int32)),
+                ("csize", C.c_int32), ("mode_ordering", C.POINTER(C.c_int32)),
+                ("mode_types", C.c_void_p), ("indices", C.POINTER(C.POINTER(C.POINTER(C.c_int32)))),
+                ("vals", C.POINTER(C.c_float)), ("vals_size", C.c_int32)]
+
+
+# name -> (restype, argtypes) of every extern "C" function in include/*.h
+_I, _I64, _P, _SZ = C.c_int32, C.c_int64, C.c_void_p, C.c_size_t
+SIGNATURES = {
+    "segtaco_version": (C.c_char_p, []),
+    "segtaco_last_error": (C.c_char_p, []),
+    "segtaco_device_available": (C.c_int, []),
+    "segtaco_autotune_heuristic": (C.c_int, [_I, _I, _I64, _I, _I, _I64, C.POINTER(Config)]),
+    "segtaco_spmm_workspace_size": (C.c_int, [_I, _I, _I64, _I, _I, C.POINTER(Config),
+                                              C.POINTER(_SZ)]),
+    "segtaco_spmm": (C.c_int, [_I, _I, _I64, _P, _P, _P, _P, _I, _I64, _P, _I64, _I,
+                               C.POINTER(Config), _P, _SZ, _P]),
+    "segtaco_spmm_partition": (C.c_int, [_I, _I, _I64, _P, _P, _I64, _I, _I, C.POINTER(Config),
+                                         _P, _SZ, _P]),
+    "segtaco_block_starts_taco": (C.c_int, [_I, _I64, _P, _I, _P, _P]),
+    "segtaco_block_starts_canonical": (C.c_int, [_I, _I64, _P, _I, _P, _P]),
+    "segtaco_merge_path": (C.c_int, [_I, _I64, _P, _I64, _P, _P, _P]),
+    "segtaco_row_ids": (C.c_int, [_I, _I64, _P, _P, _P]),
+    "segtaco_csr_validate": (C.c_int, [_I, _I, _I64, _P, _P, _P]),
+    "segtaco_spmv_workspace_size": (C.c_int, [_I, _I64, C.POINTER(_SZ)]),
+    "segtaco_spmv": (C.c_int, [_I, _I, _I64, _P, _P, _P, _P, _P, _P, _SZ, _P]),
+    "segtaco_sddmm": (C.c_int, [_I, _I, _I64, _P, _P, _P, _P, _P, _I, _I64, _I64, _I, _P, _P]),
+    "segtaco_spmspv": (C.c_int, [_I, _I, _I64, _P, _P, _P, _I, _P, _P, _P, _P]),
+    "segtaco_taco_call": (C.c_int, [_P, C.POINTER(TacoTensor), C.POINTER(TacoTensor),
+                                    C.POINTER(TacoTensor), C.POINTER(TacoTensor)]),
+    "segtaco_taco_timer_ms": (C.c_float, []),
+    "segtaco_taco_release": (None, []),
+    "segtaco_taco_num_names": (C.c_int, []),
+    "segtaco_taco_name": (C.c_char_p, [C.c_int]),
+}
+
+_lib = None
+
+
+def lib():
+    """Load libsegtaco.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise SegtacoError(EINVAL, "libsegtaco.so not built (run segtaco_gb300/build.py): %s"
+                               % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    return lib().segtaco_last_error().decode()
+
+
+def check(status: int) -> None:
+    if status != OK:
+        raise SegtacoError(status, last_error())
+
+
+def version() -> str:
+    return lib().segtaco_version().decode()
+
+
+def device_available() -> bool:
+    return bool(lib().segtaco_device_available())
+
+
+def taco_names():
+    L = lib()
+    return [L.segtaco_taco_name(i).decode() for i in range(L.segtaco_taco_num_names())]

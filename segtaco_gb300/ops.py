@@ -1,0 +1,166 @@
+"""Device-level operations over the C ABI, with torch tensors as device memory.
+
+torch only allocates device memory and names streams here; every computation
+is a call into libsegtaco.so.  Tensors must be CUDA, contiguous (dense
+operands may be row-strided), and index arrays int32.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+
+import numpy as np
+import torch
+
+from . import native as N
+
+
+def _ptr(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _stream(stream):
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return C.c_void_p(stream.cuda_stream)
+
+
+def _dense_dtype(t: torch.Tensor) -> int:
+    if t.dtype == torch.float32:
+        return N.F32
+    if t.dtype == torch.bfloat16:
+        return N.BF16
+    raise N.SegtacoError(N.EINVAL, "dense operand must be float32 or bfloat16, got %s" % t.dtype)
+
+
+@dataclasses.dataclass
+class DeviceCSR:
+    """A CSR matrix resident in device memory."""
+    row_ptr: torch.Tensor
+    col: torch.Tensor
+    val: torch.Tensor | None
+    M: int
+    K: int
+
+    @property
+    def nnz(self) -> int:
+        return int(self.col.shape[0])
+
+    @classmethod
+    def from_host(cls, csr, device="cuda", with_values=True):
+        rp = torch.from_numpy(np.ascontiguousarray(csr.row_ptr, np.int32)).to(device)
+        col = torch.from_numpy(np.ascontiguousarray(csr.col, np.int32)).to(device)
+        val = None
+        if with_values and csr.val is not None:
+            val = torch.from_numpy(np.ascontiguousarray(csr.val, np.float32)).to(device)
+        return cls(rp, col, val, int(csr.M), int(csr.K))
+
+    def nbytes(self) -> int:
+        n = self.row_ptr.numel() * 4 + self.col.numel() * 4
+        return n + (0 if self.val is None else self.val.numel() * 4)
+
+
+def spmm_workspace_size(A: DeviceCSR, n: int, b_dtype=N.F32, config: N.Config | None = None) -> int:
+    out = C.c_size_t(0)
+    N.check(N.lib().segtaco_spmm_workspace_size(A.M, A.K, A.nnz, n, b_dtype,
+                                                C.byref(config) if config else None,
+                                                C.byref(out)))
+    return out.value
+
+
+def spmm(A: DeviceCSR, B: torch.Tensor, C_out: torch.Tensor | None = None,
+         config: N.Config | None = None, workspace: torch.Tensor | None = None,
+         stream=None) -> torch.Tensor:
+    """C = A @ B (B float32 or bfloat16, K x N row-major; C float32 M x N)."""
+    if B.dim() != 2 or B.shape[0] != A.K:
+        raise N.SegtacoError(N.EINVAL, "B must be K x N with K = %d" % A.K)
+    n = int(B.shape[1])
+    if C_out is None:
+        C_out = torch.empty((A.M, n), dtype=torch.float32, device=B.device)
+    ws_ptr, ws_bytes = None, 0
+    if workspace is not None:
+        ws_ptr, ws_bytes = _ptr(workspace), workspace.numel() * workspace.element_size()
+    N.check(N.lib().segtaco_spmm(A.M, A.K, A.nnz, _ptr(A.row_ptr), _ptr(A.col), _ptr(A.val),
+                                 _ptr(B), _dense_dtype(B), B.stride(0), _ptr(C_out),
+                                 C_out.stride(0), n, C.byref(config) if config else None,
+                                 ws_ptr, ws_bytes, _stream(stream)))
+    return C_out
+
+
+def spmm_partition(A: DeviceCSR, C_out: torch.Tensor, config: N.Config, workspace: torch.Tensor,
+                   b_dtype=N.F32, stream=None) -> None:
+    """First half of spmm(): partition + zeroing of split rows of C_out; follow
+    with spmm(..., config with FLAG_PARTITION_READY, same workspace)."""
+    N.check(N.lib().segtaco_spmm_partition(A.M, A.K, A.nnz, _ptr(A.row_ptr), _ptr(C_out),
+                                           C_out.stride(0), int(C_out.shape[1]), b_dtype,
+                                           C.byref(config), _ptr(workspace),
+                                           workspace.numel() * workspace.element_size(),
+                                           _stream(stream)))
+
+
+def spmv(A: DeviceCSR, x: torch.Tensor, y: torch.Tensor | None = None, stream=None):
+    if y is None:
+        y = torch.empty(A.M, dtype=torch.float32, device=x.device)
+    N.check(N.lib().segtaco_spmv(A.M, A.K, A.nnz, _ptr(A.row_ptr), _ptr(A.col), _ptr(A.val),
+                                 _ptr(x), _ptr(y), None, 0, _stream(stream)))
+    return y
+
+
+def sddmm(A: DeviceCSR, X: torch.Tensor, Y: torch.Tensor, out: torch.Tensor | None = None,
+          stream=None):
+    """out[p] = A.val[p] * <X[i], Y[j]> over A's pattern (X: M x D, Y: K x D)."""
+    if out is None:
+        out = torch.empty(A.nnz, dtype=torch.float32, device=X.device)
+    dt = _dense_dtype(X)
+    if _dense_dtype(Y) != dt:
+        raise N.SegtacoError(N.EINVAL, "X and Y must have the same dtype")
+    N.check(N.lib().segtaco_sddmm(A.M, A.K, A.nnz, _ptr(A.row_ptr), _ptr(A.col), _ptr(A.val),
+                                  _ptr(X), _ptr(Y), dt, X.stride(0), Y.stride(0), int(X.shape[1]),
+                                  _ptr(out), _stream(stream)))
+    return out
+
+
+def spmspv(At: DeviceCSR, x_idx: torch.Tensor, x_val: torch.Tensor, m: int,
+           y: torch.Tensor | None = None, stream=None):
+    """y = A x for sparse x; At is the CSR of A^T (At.M = columns of A), m = rows of A."""
+    if y is None:
+        y = torch.empty(m, dtype=torch.float32, device=x_val.device)
+    N.check(N.lib().segtaco_spmspv(m, At.M, At.nnz, _ptr(At.row_ptr), _ptr(At.col), _ptr(At.val),
+                                   int(x_idx.shape[0]), _ptr(x_idx), _ptr(x_val), _ptr(y),
+                                   _stream(stream)))
+    return y
+
+
+def block_starts_taco(A: DeviceCSR, P: int, stream=None):
+    out = torch.empty((A.nnz + P - 1) // P + 1, dtype=torch.int32, device=A.row_ptr.device)
+    N.check(N.lib().segtaco_block_starts_taco(A.M, A.nnz, _ptr(A.row_ptr), P, _ptr(out),
+                                              _stream(stream)))
+    return out
+
+
+def block_starts_canonical(A: DeviceCSR, P: int, stream=None):
+    out = torch.empty((A.nnz + P - 1) // P + 1, dtype=torch.int32, device=A.row_ptr.device)
+    N.check(N.lib().segtaco_block_starts_canonical(A.M, A.nnz, _ptr(A.row_ptr), P, _ptr(out),
+                                                   _stream(stream)))
+    return out
+
+
+def merge_path(A: DeviceCSR, D: int, stream=None):
+    nch = max(1, (A.M + A.nnz + D - 1) // D)
+    xs = torch.empty(nch + 1, dtype=torch.int32, device=A.row_ptr.device)
+    ys = torch.empty(nch + 1, dtype=torch.int32, device=A.row_ptr.device)
+    N.check(N.lib().segtaco_merge_path(A.M, A.nnz, _ptr(A.row_ptr), D, _ptr(xs), _ptr(ys),
+                                       _stream(stream)))
+    return xs, ys
+
+
+def row_ids(A: DeviceCSR, stream=None):
+    out = torch.empty(max(1, A.nnz), dtype=torch.int32, device=A.row_ptr.device)
+    N.check(N.lib().segtaco_row_ids(A.M, A.nnz, _ptr(A.row_ptr), _ptr(out), _stream(stream)))
+    return out[: A.nnz]
+
+
+def csr_validate(A: DeviceCSR, stream=None):
+    """Raises SegtacoError(EINVAL) if the device CSR is malformed."""
+    N.check(N.lib().segtaco_csr_validate(A.M, A.K, A.nnz, _ptr(A.row_ptr), _ptr(A.col),
+                                         _stream(stream)))

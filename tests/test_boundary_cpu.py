@@ -1,0 +1,139 @@
+"""The C-ABI library: loads, exports every symbol include/*.h declares, and
+validates arguments on the host (no device work happens in these tests)."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import pytest
+
+from segtaco_gb300 import native as N
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+INCLUDE = os.path.join(ROOT, "include")
+
+
+def _header(name):
+    with open(os.path.join(INCLUDE, name)) as f:
+        return f.read()
+
+
+def c_abi_names():
+    names = set()
+    for h in ("segtaco.h", "segtaco_taco.h"):
+        txt = re.sub(r"/\*.*?\*/", "", _header(h), flags=re.S)
+        names |= set(re.findall(r"\b(segtaco_[a-z0-9_]+)\s*\(", txt))
+    return sorted(names)
+
+
+def cxx_names():
+    txt = _header("segtaco_taco.h")
+    spmm = re.findall(r"^SEGTACO_SPMM_DECL\((\w+)\)", txt, flags=re.M)
+    side = ["spmv_csr_gpu_taco", "sddmm_csr_gpu_taco", "sddmm_csr_gpu_warp", "spmspv_csr_gpu_taco",
+            "get_gpu_timer_result"]
+    return spmm, side
+
+
+def test_library_loads(native_lib):
+    assert N.version().startswith("segtaco-gb300")
+
+
+@pytest.mark.parametrize("name", c_abi_names())
+def test_c_symbol_exported(native_lib, name):
+    assert hasattr(native_lib, name), name
+    assert name in N.SIGNATURES, "ctypes signature missing for " + name
+
+
+def test_cxx_dropin_symbols_exported(native_lib):
+    spmm, side = cxx_names()
+    # gpu_kernels.cuh:11-93 declares 79 SpMM names; two more are defined there.
+    assert len(spmm) == 81
+    out = subprocess.run(["nm", "-D", "--defined-only", "-C", N.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    exported = set(re.findall(r"\b(\w+)\(taco_tensor_t\*", out))
+    exported |= set(re.findall(r"\b(get_gpu_timer_result)\(\)", out))
+    for name in spmm + side:
+        assert name in exported, name
+    # and the names are the C++ (mangled) ones a segTACO driver links against
+    raw = subprocess.run(["nm", "-D", "--defined-only", N.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    assert "_Z10spmm_rb_srP13taco_tensor_tS0_S0_" in raw
+    assert "_Z20get_gpu_timer_resultv" in raw
+
+
+def test_taco_name_table_covers_every_declared_name(native_lib):
+    spmm, side = cxx_names()
+    table = N.taco_names()
+    assert set(spmm) | set(side[:4]) == set(table)
+
+
+def test_struct_layouts_match_the_c_headers(tmp_path):
+    """ctypes mirrors of segtaco_config and taco_tensor_t have the C layout."""
+    src = tmp_path / "layout.c"
+    src.write_text("""
+#include <stddef.h>
+#include <stdio.h>
+#include "segtaco.h"
+#include "segtaco_taco.h"
+int main(void) {
+  printf("%zu %zu %zu %zu %zu\\n", sizeof(segtaco_config), sizeof(struct taco_tensor_t),
+         offsetof(struct taco_tensor_t, indices), offsetof(struct taco_tensor_t, vals),
+         offsetof(struct taco_tensor_t, vals_size));
+  return 0;
+}
+""")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", INCLUDE, str(src), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    assert got == [C.sizeof(N.Config), C.sizeof(N.TacoTensor), N.TacoTensor.indices.offset,
+                   N.TacoTensor.vals.offset, N.TacoTensor.vals_size.offset]
+
+
+def test_argument_errors_without_device(native_lib):
+    L = native_lib
+    # negative sizes are rejected before any CUDA call
+    st = L.segtaco_spmm(-1, 4, 0, None, None, None, None, N.F32, 4, None, 4, 4, None, None, 0, None)
+    assert st == N.EINVAL and "negative" in N.last_error()
+    # empty problem: nothing to do, success
+    assert L.segtaco_spmm(0, 4, 0, None, None, None, None, N.F32, 4, None, 4, 4, None, None, 0,
+                          None) == N.OK
+    st = L.segtaco_spmm(4, 4, 3, C.c_void_p(16), None, None, None, N.F32, 4, None, 4, 4, None,
+                        None, 0, None)
+    assert st == N.EINVAL and "col is NULL" in N.last_error()
+    st = L.segtaco_spmm(4, 4, 0, C.c_void_p(16), C.c_void_p(16), None, C.c_void_p(16), 7, 4,
+                        C.c_void_p(16), 4, 4, None, None, 0, None)
+    assert st == N.EINVAL and "dtype" in N.last_error()
+    st = L.segtaco_spmm(4, 4, 0, C.c_void_p(16), C.c_void_p(16), None, C.c_void_p(16), N.F32, 2,
+                        C.c_void_p(16), 4, 4, None, None, 0, None)
+    assert st == N.EINVAL and "ldb" in N.last_error()
+    bad = N.Config.make(schedule=9)
+    st = L.segtaco_spmm(4, 4, 0, C.c_void_p(256), C.c_void_p(256), None, C.c_void_p(256), N.F32,
+                        4, C.c_void_p(256), 4, 4, C.byref(bad), None, 0, None)
+    assert st == N.EINVAL and "schedule" in N.last_error()
+    assert L.segtaco_taco_call(b"no_such_kernel", None, None, None, None) == N.EINVAL
+
+
+def test_workspace_and_heuristic(native_lib):
+    L = native_lib
+    out = C.c_size_t()
+    cfg = N.Config.make(schedule="eb_sr", items_per_unit=256)
+    assert L.segtaco_spmm_workspace_size(1000, 1000, 20000, 128, N.F32, C.byref(cfg),
+                                         C.byref(out)) == N.OK
+    nch = (1000 + 20000 + 255) // 256
+    assert out.value >= 2 * (nch + 1) * 4
+    cfg = N.Config.make(schedule="rb_sr")
+    assert L.segtaco_spmm_workspace_size(1000, 1000, 20000, 128, N.F32, C.byref(cfg),
+                                         C.byref(out)) == N.OK
+    assert out.value == 0
+    h = N.Config()
+    assert L.segtaco_autotune_heuristic(16384, 16384, 262144, 32, N.F32, 16, C.byref(h)) == N.OK
+    assert h.schedule == N.RB_SR
+    assert L.segtaco_autotune_heuristic(10**6, 10**6, 2 * 10**7, 128, N.F32, 48679,
+                                        C.byref(h)) == N.OK
+    assert h.schedule == N.EB_SR
+
+
+def test_device_available_is_a_query(native_lib):
+    # never raises; 0 on a host without a GPU, 1 on the GB300
+    assert native_lib.segtaco_device_available() in (0, 1)

@@ -1,0 +1,90 @@
+"""SpMV, SDDMM and SpMSpV parity against the oracle and segTACO's own CPU
+outputs (golden), through the C ABI."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden_cases, load_golden
+from gpu_util import TOL, dev, small_cases, to_torch_bf16
+from oracle import oracle as O
+from segtaco_gb300 import ops, synth
+
+pytestmark = pytest.mark.gpu
+CASES = small_cases()
+
+
+def check_vec(got, ref, bound, tol=TOL):
+    if ref.size:
+        err = O.max_bound_err(got, ref, bound)
+        assert err <= tol, err
+
+
+@pytest.mark.parametrize("name", golden_cases("spmm_"))
+def test_spmv_golden(cuda, name):
+    d = load_golden("spmm_", name)
+    A = synth.CSR(d["row_ptr"], d["col"], d["val"], int(d["M"]), int(d["K"]))
+    y = ops.spmv(dev(A), torch.from_numpy(d["x"]).cuda()).cpu().numpy()
+    ref = O.spmv_f64(A.row_ptr, A.col, A.val, d["x"])
+    S = O.spmm_absbound(A.row_ptr, A.col, A.val, d["x"].reshape(-1, 1)).reshape(-1)
+    check_vec(y, ref, S)
+    check_vec(y, d["y_eigen"].astype(np.float64), S, 2 * TOL)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_spmv_small(cuda, name):
+    A = CASES[name]
+    x = synth.dense(A.K, 1, seed=3).reshape(-1)
+    y = ops.spmv(dev(A), torch.from_numpy(x).cuda()).cpu().numpy()
+    S = O.spmm_absbound(A.row_ptr, A.col, A.val, x.reshape(-1, 1)).reshape(-1)
+    check_vec(y, O.spmv_f64(A.row_ptr, A.col, A.val, x), S)
+
+
+def test_spmv_full_power_law(cuda):
+    A = synth.power_law(seed=0)
+    x = synth.dense(A.K, 1, seed=2).reshape(-1)
+    y = ops.spmv(dev(A), torch.from_numpy(x).cuda()).cpu().numpy()
+    S = O.spmm_absbound(A.row_ptr, A.col, A.val, x.reshape(-1, 1)).reshape(-1)
+    check_vec(y, O.spmv_f64(A.row_ptr, A.col, A.val, x), S)
+
+
+@pytest.mark.parametrize("name", golden_cases("sddmm_"))
+def test_sddmm_golden(cuda, name):
+    d = load_golden("sddmm_", name)
+    A = synth.CSR(d["row_ptr"], d["col"], d["val"], int(d["M"]), int(d["K"]))
+    out = ops.sddmm(dev(A), torch.from_numpy(d["X"]).cuda(), torch.from_numpy(d["Y"]).cuda())
+    _, bound = O.sddmm_f64(A.row_ptr, A.col, A.val, d["X"], d["Y"])
+    check_vec(out.cpu().numpy(), d["out"], bound)  # sddmm_csr_cpu_taco_ref, in double
+
+
+@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("D", [1, 5, 16, 64, 100])
+def test_sddmm_small(cuda, name, D):
+    A = CASES[name]
+    X = synth.dense(A.M, D, seed=4)
+    Y = synth.dense(A.K, D, seed=5)
+    out = ops.sddmm(dev(A), torch.from_numpy(X).cuda(), torch.from_numpy(Y).cuda())
+    ref, bound = O.sddmm_f64(A.row_ptr, A.col, A.val, X, Y)
+    check_vec(out.cpu().numpy(), ref, bound)
+
+
+@pytest.mark.parametrize("D", [8, 64])
+def test_sddmm_bf16(cuda, D):
+    A = CASES["banded"]
+    X = synth.to_bf16_bits(synth.dense(A.M, D, seed=6))
+    Y = synth.to_bf16_bits(synth.dense(A.K, D, seed=7))
+    out = ops.sddmm(dev(A), to_torch_bf16(X), to_torch_bf16(Y))
+    ref, bound = O.sddmm_f64(A.row_ptr, A.col, A.val, X, Y, bf16=True)
+    check_vec(out.cpu().numpy(), ref, bound)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_spmspv(cuda, name):
+    A = CASES[name]
+    At = A.transpose()
+    rng = np.random.default_rng(1)
+    nx = max(1, A.K // 10)
+    idx = rng.permutation(A.K)[:nx].astype(np.int32)
+    xv = rng.uniform(-1, 1, nx).astype(np.float32)
+    y = ops.spmspv(dev(At), torch.from_numpy(idx).cuda(), torch.from_numpy(xv).cuda(), A.M)
+    ref, bound = O.spmspv_f64(At.row_ptr, At.col, At.val, A.M, idx, xv)
+    check_vec(y.cpu().numpy(), ref, bound)
