@@ -48,6 +48,10 @@ def make_workload(name):
         A = synth.power_law(seed=0)
         N = 128
         desc = "power-law SpMM: A 1Mx1M Zipf(1.8) cap 50000, 2% empty rows, N=128, fp32"
+    elif name == "power_law_quarter":
+        A = synth.power_law(250_000, 250_000, seed=0)
+        N = 128
+        desc = "power-law SpMM (quarter size, for profiling): A 250kx250k Zipf(1.8) cap 50000, N=128, fp32"
     elif name == "uniform16":
         A = synth.uniform_rows(seed=0)
         N = 32
@@ -368,7 +372,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="power_law", choices=["power_law", "uniform16", "banded"])
+    ap.add_argument("--workload", default="power_law", choices=["power_law", "power_law_quarter", "uniform16", "banded"])
     ap.add_argument("--schedule", default="auto", choices=["auto", "rb_sr", "rb_pr", "eb_sr", "eb_pr"])
     ap.add_argument("--col-tile", type=int, default=0)
     ap.add_argument("--items", type=int, default=0)

@@ -169,11 +169,14 @@ int run_spmm_planned(const SpmmPlan &plan, int M, int K, long long nnz, const in
 long long spmv_tile_items();
 long long sddmm_block_nnz();
 
-static int check_csr_args(int M, int K, long long nnz, const int *row_ptr, const int *col) {
+// Host-side checks of the CSR arguments; `need_col` is false for the calls
+// that only read row_ptr (partitions, row ids).
+static int check_csr_args(int M, int K, long long nnz, const int *row_ptr, const int *col,
+                          bool need_col = true) {
   if (M < 0 || K < 0 || nnz < 0) return set_error(SEGTACO_EINVAL, "negative size");
   if (nnz > 0x7fffffffLL) return set_error(SEGTACO_EINVAL, "nnz exceeds int32 indices");
   if (M > 0 && row_ptr == nullptr) return set_error(SEGTACO_EINVAL, "row_ptr is NULL");
-  if (nnz > 0 && col == nullptr) return set_error(SEGTACO_EINVAL, "col is NULL");
+  if (need_col && nnz > 0 && col == nullptr) return set_error(SEGTACO_EINVAL, "col is NULL");
   return SEGTACO_OK;
 }
 
@@ -256,7 +259,7 @@ int segtaco_spmm(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr, cons
 int segtaco_spmm_partition(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr, float *C,
                            int64_t ldc, int32_t N, int32_t b_dtype, const segtaco_config *cfg,
                            void *workspace, size_t workspace_bytes, void *stream) {
-  SEGTACO_TRY(check_csr_args(M, K, nnz, row_ptr, nullptr));
+  SEGTACO_TRY(check_csr_args(M, K, nnz, row_ptr, nullptr, false));
   if (M == 0 || N == 0) return SEGTACO_OK;
   if (C == nullptr || ldc < N) return set_error(SEGTACO_EINVAL, "C is NULL or ldc < N");
   SpmmPlan plan;
@@ -274,7 +277,7 @@ int segtaco_spmm_partition(int32_t M, int32_t K, int64_t nnz, const int32_t *row
 
 int segtaco_block_starts_taco(int32_t M, int64_t nnz, const int32_t *row_ptr, int32_t P,
                               int32_t *out, void *stream) {
-  SEGTACO_TRY(check_csr_args(M, 0, nnz, row_ptr, nullptr));
+  SEGTACO_TRY(check_csr_args(M, 0, nnz, row_ptr, nullptr, false));
   if (P <= 0 || out == nullptr) return set_error(SEGTACO_EINVAL, "P must be > 0, out non-NULL");
   const long long nblk = (nnz + P - 1) / P;
   return launch_block_starts_taco(row_ptr, M, P, nblk, out, static_cast<cudaStream_t>(stream));
@@ -282,7 +285,7 @@ int segtaco_block_starts_taco(int32_t M, int64_t nnz, const int32_t *row_ptr, in
 
 int segtaco_block_starts_canonical(int32_t M, int64_t nnz, const int32_t *row_ptr, int32_t P,
                                    int32_t *out, void *stream) {
-  SEGTACO_TRY(check_csr_args(M, 0, nnz, row_ptr, nullptr));
+  SEGTACO_TRY(check_csr_args(M, 0, nnz, row_ptr, nullptr, false));
   if (P <= 0 || out == nullptr) return set_error(SEGTACO_EINVAL, "P must be > 0, out non-NULL");
   const long long nblk = (nnz + P - 1) / P;
   return launch_block_starts_canonical(row_ptr, M, P, nblk, out,
@@ -291,7 +294,7 @@ int segtaco_block_starts_canonical(int32_t M, int64_t nnz, const int32_t *row_pt
 
 int segtaco_merge_path(int32_t M, int64_t nnz, const int32_t *row_ptr, int64_t D, int32_t *out_x,
                        int32_t *out_y, void *stream) {
-  SEGTACO_TRY(check_csr_args(M, 0, nnz, row_ptr, nullptr));
+  SEGTACO_TRY(check_csr_args(M, 0, nnz, row_ptr, nullptr, false));
   if (D <= 0 || !out_x || !out_y) return set_error(SEGTACO_EINVAL, "D must be > 0, outputs non-NULL");
   long long nch = ((long long)M + nnz + D - 1) / D;
   if (nch < 1) nch = 1;
@@ -300,7 +303,7 @@ int segtaco_merge_path(int32_t M, int64_t nnz, const int32_t *row_ptr, int64_t D
 }
 
 int segtaco_row_ids(int32_t M, int64_t nnz, const int32_t *row_ptr, int32_t *out, void *stream) {
-  SEGTACO_TRY(check_csr_args(M, 0, nnz, row_ptr, nullptr));
+  SEGTACO_TRY(check_csr_args(M, 0, nnz, row_ptr, nullptr, false));
   if (nnz > 0 && out == nullptr) return set_error(SEGTACO_EINVAL, "out is NULL");
   return launch_row_ids(row_ptr, M, out, static_cast<cudaStream_t>(stream));
 }
