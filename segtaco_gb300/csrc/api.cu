@@ -80,22 +80,32 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
            ((uintptr_t)C % (vc * 4)) == 0;
   };
   while (V > 1 && !fits(V)) V >>= 1;
-  // Slab width W = G*V columns: a 128-byte row segment by default (32 fp32 /
-  // 64 bf16 columns), never wider than N needs.
-  int W = c.col_tile > 0 ? c.col_tile : 128 / esz;
-  if (W % V != 0) W = ((W + V - 1) / V) * V;
-  int G = W / V;
-  if (G < 1) G = 1;
-  if (G > 32) G = 32;
-  while (!is_pow2(G)) --G;
-  while (G > 1 && (G / 2) * V >= N) G >>= 1;  // no idle half-groups
-  W = G * V;
   int schedule = c.schedule;
   // Without row-length statistics the merge path is the safe default: its
   // work per unit is bounded whatever the row-length skew.
-  if (schedule == SEGTACO_AUTO) schedule = SEGTACO_EB_SR;
+  if (schedule == SEGTACO_AUTO) schedule = SEGTACO_EB_PR;
   if (schedule < SEGTACO_RB_SR || schedule > SEGTACO_EB_PR)
     return set_error(SEGTACO_EINVAL, "unknown schedule %d", schedule);
+  const bool sequential = schedule == SEGTACO_RB_SR || schedule == SEGTACO_EB_SR;
+  // Slab width W = G*V columns.  Sequential schedules use one slot (G = 32);
+  // parallel ones use P = 32/G >= 2 slots, by default a 128-byte B segment per
+  // nonzero (32 fp32 / 64 bf16 columns).
+  int G;
+  if (sequential) {
+    G = 32;
+    if (c.col_tile > 0 && c.vec <= 0) {
+      // A requested slab width picks the vector width (W = 32*V).
+      while (V > 1 && 32 * V > c.col_tile) V >>= 1;
+    }
+  } else {
+    int W = c.col_tile > 0 ? c.col_tile : 128 / esz;
+    G = W / V;
+    if (G < 1) G = 1;
+    if (G > 16) G = 16;
+    while (!is_pow2(G)) --G;
+    while (G > 1 && (G / 2) * V >= N) G >>= 1;  // no idle half-slots
+  }
+  const int W = G * V;
   plan->schedule = schedule;
   plan->V = V;
   plan->G = G;
@@ -104,10 +114,10 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
   plan->l2_hints = (c.flags & SEGTACO_FLAG_L2_HINTS) != 0;
   plan->rows_per_unit = c.rows_per_unit > 0 ? c.rows_per_unit : 1;
   plan->items_per_unit = 0;
-  plan->nchunks = 0;
+  plan->nchunks = (M + plan->rows_per_unit - 1) / plan->rows_per_unit;  // rb: row blocks
   plan->workspace = 0;
   if (schedule == SEGTACO_EB_SR || schedule == SEGTACO_EB_PR) {
-    long long D = c.items_per_unit > 0 ? c.items_per_unit : (schedule == SEGTACO_EB_SR ? 256 : 512);
+    long long D = c.items_per_unit > 0 ? c.items_per_unit : 512;
     if (D < 1) D = 1;
     const long long total = (long long)M + nnz;
     long long nch = (total + D - 1) / D;
@@ -126,7 +136,6 @@ int run_spmm_planned(const SpmmPlan &plan, int M, int K, long long nnz, const in
                      bool partition_ready) {
   if (M == 0 || N == 0) return SEGTACO_OK;
   SpmmLaunch L;
-  L.schedule = plan.schedule;
   L.dtype = b_dtype;
   L.V = plan.V;
   L.G = plan.G;
@@ -144,23 +153,19 @@ int run_spmm_planned(const SpmmPlan &plan, int M, int K, long long nnz, const in
   L.ldc = ldc;
   L.part_x = px;
   L.part_y = py;
+  L.units = plan.nchunks;
+  L.rows_per_unit = (int)plan.rows_per_unit;
   const bool bf16 = b_dtype == SEGTACO_BF16;
   switch (plan.schedule) {
     case SEGTACO_RB_SR:
-      L.units = plan.rows_per_unit;
-      return bf16 ? launch_spmm_rb_sr_bf16(L, s) : launch_spmm_rb_sr_f32(L, s);
     case SEGTACO_RB_PR:
-      L.units = plan.rows_per_unit;
-      return bf16 ? launch_spmm_rb_pr_bf16(L, s) : launch_spmm_rb_pr_f32(L, s);
+      return bf16 ? launch_spmm_bf16_rows(L, s) : launch_spmm_f32_rows(L, s);
     case SEGTACO_EB_SR:
     case SEGTACO_EB_PR:
       if (!partition_ready)
         SEGTACO_TRY(launch_merge_path(row_ptr, M, nnz, plan.items_per_unit, plan.nchunks, px, py,
                                       C, ldc, N, s));
-      L.units = plan.nchunks;
-      if (plan.schedule == SEGTACO_EB_SR)
-        return bf16 ? launch_spmm_eb_sr_bf16(L, s) : launch_spmm_eb_sr_f32(L, s);
-      return bf16 ? launch_spmm_eb_pr_bf16(L, s) : launch_spmm_eb_pr_f32(L, s);
+      return bf16 ? launch_spmm_bf16_chunks(L, s) : launch_spmm_f32_chunks(L, s);
     default:
       return set_error(SEGTACO_EINVAL, "unknown schedule %d", plan.schedule);
   }
@@ -206,7 +211,7 @@ int segtaco_autotune_heuristic(int32_t M, int32_t K, int64_t nnz, int32_t N, int
   const double mean = M > 0 ? (double)nnz / M : 0.0;
   // Row-balanced sequential when rows are short and even; merge path otherwise.
   const bool even = max_row_len >= 0 && mean > 0.0 && (double)max_row_len <= 4.0 * mean + 8.0;
-  cfg->schedule = even ? SEGTACO_RB_SR : SEGTACO_EB_SR;
+  cfg->schedule = even ? SEGTACO_RB_PR : SEGTACO_EB_PR;
   const int esz = b_dtype == SEGTACO_BF16 ? 2 : 4;
   // Whole B fits comfortably in L2: one slab as wide as N (up to 128 columns).
   const double bbytes = (double)K * N * esz;

@@ -108,51 +108,77 @@ __device__ __forceinline__ uint32_t ld_u1(const uint16_t *p, uint64_t pol) {
 __device__ __forceinline__ float bf16lo(uint32_t w) { return __uint_as_float(w << 16); }
 __device__ __forceinline__ float bf16hi(uint32_t w) { return __uint_as_float(w & 0xffff0000u); }
 
-// Load V consecutive dense elements starting at p into float registers.
+// V consecutive dense elements as one raw vector load (kept raw in registers
+// until used, so a bf16 x 8 load costs 4 registers, like an fp32 x 4 one).
 // float: V in {1,2,4}; bf16 (uint16_t): V in {1,2,4,8}.
-template <typename BT, int V, bool kHint> struct DenseLoad;
+template <typename BT, int V> struct Dense;
 
-template <bool H> struct DenseLoad<float, 4, H> {
-  static __device__ __forceinline__ void run(const float *p, float (&o)[4], uint64_t pol) {
-    float4 t = ld_b4<H>(p, pol);
-    o[0] = t.x; o[1] = t.y; o[2] = t.z; o[3] = t.w;
+template <> struct Dense<float, 4> {
+  using raw_t = float4;
+  static __device__ __forceinline__ raw_t load(const float *p, uint64_t pol) {
+    return ld_b4<true>(p, pol);
+  }
+  static __device__ __forceinline__ float get(const raw_t &r, int v) {
+    return v == 0 ? r.x : v == 1 ? r.y : v == 2 ? r.z : r.w;
   }
 };
-template <bool H> struct DenseLoad<float, 2, H> {
-  static __device__ __forceinline__ void run(const float *p, float (&o)[2], uint64_t pol) {
-    float2 t = ld_b2<H>(p, pol);
-    o[0] = t.x; o[1] = t.y;
+template <> struct Dense<float, 2> {
+  using raw_t = float2;
+  static __device__ __forceinline__ raw_t load(const float *p, uint64_t pol) {
+    return ld_b2<true>(p, pol);
+  }
+  static __device__ __forceinline__ float get(const raw_t &r, int v) { return v == 0 ? r.x : r.y; }
+};
+template <> struct Dense<float, 1> {
+  using raw_t = float;
+  static __device__ __forceinline__ raw_t load(const float *p, uint64_t pol) {
+    return ld_b1<true>(p, pol);
+  }
+  static __device__ __forceinline__ float get(const raw_t &r, int) { return r; }
+};
+template <> struct Dense<uint16_t, 8> {
+  using raw_t = uint4;
+  static __device__ __forceinline__ raw_t load(const uint16_t *p, uint64_t pol) {
+    return ld_u4<true>(p, pol);
+  }
+  static __device__ __forceinline__ float get(const raw_t &r, int v) {
+    const uint32_t w = v < 2 ? r.x : v < 4 ? r.y : v < 6 ? r.z : r.w;
+    return (v & 1) ? bf16hi(w) : bf16lo(w);
   }
 };
-template <bool H> struct DenseLoad<float, 1, H> {
-  static __device__ __forceinline__ void run(const float *p, float (&o)[1], uint64_t pol) {
-    o[0] = ld_b1<H>(p, pol);
+template <> struct Dense<uint16_t, 4> {
+  using raw_t = uint2;
+  static __device__ __forceinline__ raw_t load(const uint16_t *p, uint64_t pol) {
+    return ld_u2<true>(p, pol);
+  }
+  static __device__ __forceinline__ float get(const raw_t &r, int v) {
+    const uint32_t w = v < 2 ? r.x : r.y;
+    return (v & 1) ? bf16hi(w) : bf16lo(w);
   }
 };
-template <bool H> struct DenseLoad<uint16_t, 8, H> {
-  static __device__ __forceinline__ void run(const uint16_t *p, float (&o)[8], uint64_t pol) {
-    uint4 t = ld_u4<H>(p, pol);
-    o[0] = bf16lo(t.x); o[1] = bf16hi(t.x); o[2] = bf16lo(t.y); o[3] = bf16hi(t.y);
-    o[4] = bf16lo(t.z); o[5] = bf16hi(t.z); o[6] = bf16lo(t.w); o[7] = bf16hi(t.w);
+template <> struct Dense<uint16_t, 2> {
+  using raw_t = uint32_t;
+  static __device__ __forceinline__ raw_t load(const uint16_t *p, uint64_t pol) {
+    return ld_u1<true>(p, pol);
+  }
+  static __device__ __forceinline__ float get(const raw_t &r, int v) {
+    return (v & 1) ? bf16hi(r) : bf16lo(r);
   }
 };
-template <bool H> struct DenseLoad<uint16_t, 4, H> {
-  static __device__ __forceinline__ void run(const uint16_t *p, float (&o)[4], uint64_t pol) {
-    uint2 t = ld_u2<H>(p, pol);
-    o[0] = bf16lo(t.x); o[1] = bf16hi(t.x); o[2] = bf16lo(t.y); o[3] = bf16hi(t.y);
+template <> struct Dense<uint16_t, 1> {
+  using raw_t = uint32_t;
+  static __device__ __forceinline__ raw_t load(const uint16_t *p, uint64_t) {
+    return (uint32_t)__ldg(reinterpret_cast<const unsigned short *>(p));
   }
+  static __device__ __forceinline__ float get(const raw_t &r, int) { return bf16lo(r); }
 };
-template <bool H> struct DenseLoad<uint16_t, 2, H> {
-  static __device__ __forceinline__ void run(const uint16_t *p, float (&o)[2], uint64_t pol) {
-    uint32_t t = ld_u1<H>(p, pol);
-    o[0] = bf16lo(t); o[1] = bf16hi(t);
-  }
-};
-template <bool H> struct DenseLoad<uint16_t, 1, H> {
-  static __device__ __forceinline__ void run(const uint16_t *p, float (&o)[1], uint64_t pol) {
-    (void)pol;
-    unsigned short h = __ldg(reinterpret_cast<const unsigned short *>(p));
-    o[0] = __uint_as_float(((uint32_t)h) << 16);
+
+// Compatibility form used by the SDDMM kernel: load and convert at once.
+template <typename BT, int V, bool kHint> struct DenseLoad {
+  static __device__ __forceinline__ void run(const BT *p, float (&o)[V], uint64_t pol) {
+    const auto r = Dense<BT, V>::load(p, pol);
+#pragma unroll
+    for (int v = 0; v < V; ++v) o[v] = Dense<BT, V>::get(r, v);
   }
 };
 

@@ -57,9 +57,8 @@ int launch_validate(const int *row_ptr, int M, int K, long long nnz, const int *
 
 // ---- SpMM kernel launch description (spmm_*.cu) ----
 struct SpmmLaunch {
-  int schedule;  // SEGTACO_RB_SR .. SEGTACO_EB_PR
   int dtype;     // SEGTACO_F32 / SEGTACO_BF16
-  int V, G;      // vector width (elements) and lanes per group
+  int V, G;      // vector width (elements) and lanes per slot (P = 32/G slots)
   bool l2_hints;
   int M, K, N;
   long long nnz;
@@ -69,18 +68,15 @@ struct SpmmLaunch {
   long long ldb;
   float *C;
   long long ldc;
-  const int *part_x, *part_y;  // eb only
-  long long units;             // rb: rows per group (sr) / warp (pr); eb: chunk count
+  const int *part_x, *part_y;  // chunks only
+  long long units;             // warps: merge-path chunks or row blocks
+  int rows_per_unit;           // row blocks only
 };
-// One launcher per (schedule, dtype); each switches over (V, G, hints).
-int launch_spmm_rb_sr_f32(const SpmmLaunch &L, cudaStream_t s);
-int launch_spmm_rb_pr_f32(const SpmmLaunch &L, cudaStream_t s);
-int launch_spmm_eb_sr_f32(const SpmmLaunch &L, cudaStream_t s);
-int launch_spmm_eb_pr_f32(const SpmmLaunch &L, cudaStream_t s);
-int launch_spmm_rb_sr_bf16(const SpmmLaunch &L, cudaStream_t s);
-int launch_spmm_rb_pr_bf16(const SpmmLaunch &L, cudaStream_t s);
-int launch_spmm_eb_sr_bf16(const SpmmLaunch &L, cudaStream_t s);
-int launch_spmm_eb_pr_bf16(const SpmmLaunch &L, cudaStream_t s);
+// One launcher per (dense type, unit kind); each switches over (V, G).
+int launch_spmm_f32_rows(const SpmmLaunch &L, cudaStream_t s);
+int launch_spmm_f32_chunks(const SpmmLaunch &L, cudaStream_t s);
+int launch_spmm_bf16_rows(const SpmmLaunch &L, cudaStream_t s);
+int launch_spmm_bf16_chunks(const SpmmLaunch &L, cudaStream_t s);
 
 // Resolved plan of one SpMM call (api.cu).
 struct SpmmPlan {

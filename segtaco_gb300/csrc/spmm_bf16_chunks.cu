@@ -1,0 +1,9 @@
+// spmm_bf16_chunks.cu -- SpMM launcher: dense operand bf16, units = chunks.
+#include "spmm_launch.cuh"
+
+#define SEGTACO_SPMM_CASE(V, G, R)                                   \
+  case V * 100 + G:                                                  \
+    spmm_seg_kernel<uint16_t, V, G, R><<<grid, kCta, 0, s>>>(a);        \
+    break;
+
+SEGTACO_DEFINE_SPMM_LAUNCHER(launch_spmm_bf16_chunks, uint16_t, SEGTACO_VG_BF16, false)

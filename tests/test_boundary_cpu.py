@@ -128,10 +128,10 @@ def test_workspace_and_heuristic(native_lib):
     assert out.value == 0
     h = N.Config()
     assert L.segtaco_autotune_heuristic(16384, 16384, 262144, 32, N.F32, 16, C.byref(h)) == N.OK
-    assert h.schedule == N.RB_SR
+    assert h.schedule == N.RB_PR
     assert L.segtaco_autotune_heuristic(10**6, 10**6, 2 * 10**7, 128, N.F32, 48679,
                                         C.byref(h)) == N.OK
-    assert h.schedule == N.EB_SR
+    assert h.schedule == N.EB_PR
 
 
 def test_device_available_is_a_query(native_lib):
