@@ -151,6 +151,30 @@ __global__ void __launch_bounds__(kCta, V == 8 ? 3 : 4) spmm_seg_kernel(SpmmArgs
     const int nbn = y1 - pn < 32 ? y1 - pn : 32;
     const int mcn = lane < nbn ? ld_stream(a.col + pn + lane) : 0;
     const float mvn = lane < nbn ? ld_val(a.val, pn + lane) : 0.0f;
+    if (nb == 32 && p + 32 <= cend) {
+      // The whole batch lies inside row `cur`: multiply-adds only.
+#pragma unroll
+      for (int s0 = 0; s0 < S; s0 += U) {
+        typename D::raw_t b[U];
+        float vv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int t = (s0 + u) * P + slot;
+          const int j = __shfl_sync(FULL, mc, t);
+          vv[u] = __shfl_sync(FULL, mv, t);
+          b[u] = D::load(Bc + (size_t)(unsigned)j * ldb, pol);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+#pragma unroll
+          for (int v = 0; v < V; ++v) acc[v] = fmaf(vv[u], D::get(b[u], v), acc[v]);
+        }
+      }
+      nb = nbn;
+      mc = mcn;
+      mv = mvn;
+      continue;
+    }
 #pragma unroll
     for (int s0 = 0; s0 < S; s0 += U) {
       if (s0 * P >= nb) break;
