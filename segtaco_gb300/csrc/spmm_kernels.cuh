@@ -7,13 +7,18 @@
 //             block of R consecutive rows (row-balanced, rb_*);
 //   * slab  = W = G*V dense columns (blockIdx.y), G lanes x V-wide vector loads
 //             (16 B per lane for fp32 V=4 / bf16 V=8).
-// The 32 lanes form P = 32/G slots of G lanes.  The warp walks the unit's
-// nonzeros in storage order, P at a time (one per slot): slot s takes the s-th
-// nonzero of each step and reads one W-column segment of that B row.  All
-// control flow is warp-uniform: a step whose P nonzeros all lie in the current
-// row is a plain multiply-add (the fast path); a step that reaches a row end
-// takes the slow path, which folds the slots' partial sums with xor shuffles
-// and writes the row.
+// The 32 lanes form P = 32/G slots of G lanes; a slot reads one W-column
+// segment of one B row per step.  The warp walks the unit's rows in order and
+// treats each row by its length (all control flow is warp-uniform):
+//   * a row with >= 2P nonzeros (in this unit) is split over the slots: step k
+//     gives slot s the nonzero k*P + s; batches of 32 nonzeros are aligned to
+//     the row start, so the inner loop is multiply-adds only; at the row end
+//     the slots' partial sums are folded with xor shuffles and slot 0 writes;
+//   * a run of shorter rows is spread one row per slot (up to P rows whose
+//     nonzeros fit one 32-nonzero batch); each slot sums its own row and
+//     writes it, so short rows pay no fold.
+// The next batch of column indices and values is always loaded (from the next
+// row start) before the current one is used.
 //
 // Schedules (segTACO's 2x2 space, gpu_kernels.cuh:11-93):
 //   rb_sr  row blocks, P = 1 (G = 32): every lane sums its columns of a row
@@ -79,12 +84,13 @@ template <int G, int V> __device__ __forceinline__ void fold_slots(float (&r)[V]
 // a few more for their 8 accumulators and run 3 CTAs per SM.
 template <typename BT, int V, int G, bool ROWS>
 __global__ void __launch_bounds__(kCta, V == 8 ? 3 : 4) spmm_seg_kernel(SpmmArgs<BT> a) {
-  constexpr int P = 32 / G;          // slots = nonzeros per step
-  constexpr int S = G;               // steps per batch of 32 nonzeros
-  // Steps whose B loads are in flight together: 4 sixteen-byte loads or 8
-  // narrower ones per lane (raw registers: 16 at most).
+  constexpr int P = 32 / G;                 // slots
+  // Rows with >= LONG nonzeros are split over the slots (LONG <= 32, so a
+  // short row always fits one batch).
+  constexpr int LONG = P == 1 ? 0 : (2 * P < 32 ? 2 * P : 32);
+  // B loads in flight per lane: 4 sixteen-byte or 8 narrower raw vectors.
   constexpr int UL = V * (int)sizeof(BT) >= 16 ? 4 : 8;
-  constexpr int U = S < UL ? S : UL;
+  constexpr int UB = G < UL ? G : UL;       // steps per sub-batch in a split row
   using D = Dense<BT, V>;
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -101,7 +107,7 @@ __global__ void __launch_bounds__(kCta, V == 8 ? 3 : 4) spmm_seg_kernel(SpmmArgs
   const unsigned ldb = (unsigned)a.ldb;
 
   int x0, x1, y0, y1;
-  bool head_split = false;
+  bool head_split = false, tail_open = false;
   if (ROWS) {
     const long long r0 = w * a.rows_per_unit;
     x0 = (int)r0;
@@ -113,120 +119,142 @@ __global__ void __launch_bounds__(kCta, V == 8 ? 3 : 4) spmm_seg_kernel(SpmmArgs
     y0 = __ldg(a.part_y + w);
     x1 = __ldg(a.part_x + w + 1);
     y1 = __ldg(a.part_y + w + 1);
+    // Row x0 began in an earlier chunk; row x1 holds nonzeros here and ends in a later one.
     head_split = x0 < M && __ldg(a.row_ptr + x0) < y0;
+    tail_open = x1 < M && __ldg(a.row_ptr + x1) < y1;
   }
+  const int last = tail_open ? x1 : x1 - 1;  // rows of this unit: x0 .. last
 
-  // Current row and its end; lane l holds the end of row wb + l.
+  // Row ends: lane l holds the end of row wb + l (INT_MAX past the last row).
   int cur = x0, wb = x0;
   int rw = (wb + lane < M) ? __ldg(a.row_ptr + wb + 1 + lane) : INT_MAX;
-  int cend = __shfl_sync(FULL, rw, 0);
+  int cstart = y0;  // first nonzero of row `cur` inside this unit
+  // Batch buffer: lane l holds nonzero cstart + l (0 / 0.0 past the unit).
+  int mc = lane < y1 - cstart ? ld_stream(a.col + cstart + lane) : 0;
+  float mv = lane < y1 - cstart ? ld_val(a.val, cstart + lane) : 0.0f;
   float acc[V];
-  zero<V>(acc);
 
-  // Write row `cur` (the slots' sum) and move to the next row.
-  auto flush = [&]() {
-    fold_slots<G, V>(acc);
-    if (slot == 0 && active) {
-      float *dst = a.C + (long long)cur * a.ldc + col0;
-      if (!ROWS && cur == x0 && head_split)
-        atomic_add_c<V>(dst, acc);
-      else
-        store_c<V>(dst, acc);
-    }
-    zero<V>(acc);
-    ++cur;
-    if (cur - wb == 32) {
+  while (cur <= last) {
+    if (cur - wb > 32 - P) {  // keep rows cur .. cur+P-1 inside the window
       wb = cur;
       rw = (wb + lane < M) ? __ldg(a.row_ptr + wb + 1 + lane) : INT_MAX;
     }
-    cend = __shfl_sync(FULL, rw, cur - wb);
-  };
-
-  int nb = y1 - y0 < 32 ? y1 - y0 : 32;
-  int mc = lane < nb ? ld_stream(a.col + y0 + lane) : 0;
-  float mv = lane < nb ? ld_val(a.val, y0 + lane) : 0.0f;
-  for (int p = y0; p < y1; p += 32) {
-    // Indices of the next batch are loaded while this one is processed.
-    const int pn = p + 32;
-    const int nbn = y1 - pn < 32 ? y1 - pn : 32;
-    const int mcn = lane < nbn ? ld_stream(a.col + pn + lane) : 0;
-    const float mvn = lane < nbn ? ld_val(a.val, pn + lane) : 0.0f;
-    if (nb == 32 && p + 32 <= cend) {
-      // The whole batch lies inside row `cur`: multiply-adds only.
+    const int rend = min(__shfl_sync(FULL, rw, cur - wb), y1);
+    if (P == 1 || rend - cstart >= LONG) {
+      // ---- row `cur` split over the slots --------------------------------
+      zero<V>(acc);
+      for (int p = cstart; p < rend; p += 32) {
+        const int nb = rend - p < 32 ? rend - p : 32;
+        const int nxt = p + 32 < rend ? p + 32 : rend;
+        const int mcn = lane < y1 - nxt ? ld_stream(a.col + nxt + lane) : 0;
+        const float mvn = lane < y1 - nxt ? ld_val(a.val, nxt + lane) : 0.0f;
+        if (nb == 32) {
 #pragma unroll
-      for (int s0 = 0; s0 < S; s0 += U) {
-        typename D::raw_t b[U];
-        float vv[U];
+          for (int s0 = 0; s0 < G; s0 += UB) {
+            typename D::raw_t b[UB];
+            float vv[UB];
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int t = (s0 + u) * P + slot;
+            for (int u = 0; u < UB; ++u) {
+              const int t = (s0 + u) * P + slot;
+              const int j = __shfl_sync(FULL, mc, t);
+              vv[u] = __shfl_sync(FULL, mv, t);
+              b[u] = D::load(Bc + (size_t)(unsigned)j * ldb, pol);
+            }
+#pragma unroll
+            for (int u = 0; u < UB; ++u) {
+#pragma unroll
+              for (int v = 0; v < V; ++v) acc[v] = fmaf(vv[u], D::get(b[u], v), acc[v]);
+            }
+          }
+        } else {
+          for (int s0 = 0; s0 * P < nb; s0 += UB) {
+            typename D::raw_t b[UB];
+            float vv[UB];
+#pragma unroll
+            for (int u = 0; u < UB; ++u) {
+              const int t = (s0 + u) * P + slot;
+              const bool ok = t < nb;
+              const int j = __shfl_sync(FULL, mc, ok ? t : 0);
+              const float v = __shfl_sync(FULL, mv, ok ? t : 0);
+              vv[u] = ok ? v : 0.0f;
+              b[u] = D::load(Bc + (size_t)(unsigned)j * ldb, pol);
+            }
+#pragma unroll
+            for (int u = 0; u < UB; ++u) {
+              if ((s0 + u) * P + slot < nb) {
+#pragma unroll
+                for (int v = 0; v < V; ++v) acc[v] = fmaf(vv[u], D::get(b[u], v), acc[v]);
+              }
+            }
+          }
+        }
+        mc = mcn;
+        mv = mvn;
+      }
+      fold_slots<G, V>(acc);
+      if (slot == 0 && active) {
+        float *dst = a.C + (long long)cur * a.ldc + col0;
+        if (!ROWS && ((cur == x0 && head_split) || (cur == x1 && tail_open)))
+          atomic_add_c<V>(dst, acc);
+        else
+          store_c<V>(dst, acc);
+      }
+      cstart = rend;
+      ++cur;
+    } else {
+      // ---- short rows: slot s takes row cur + s -------------------------
+      const int r = cur + slot;
+      const int e = r <= last ? min(__shfl_sync(FULL, rw, r - wb), y1) : INT_MAX;
+      const int prev_end = min(__shfl_sync(FULL, rw, r - wb - 1 >= 0 ? r - wb - 1 : 0), y1);
+      const int sbeg = slot == 0 ? cstart : prev_end;
+      const int len = e - sbeg;
+      // Take the longest prefix of slots whose rows are short and fit the batch.
+      const bool ok = r <= last && len < LONG && e - cstart <= 32;
+      unsigned leaders = 0;
+#pragma unroll
+      for (int q = 0; q < P; ++q) leaders |= 1u << (q * G);
+      const unsigned bad = ~__ballot_sync(FULL, ok) & leaders;
+      const int k = bad ? (__ffs(bad) - 1) / G : P;  // >= 1: slot 0 always qualifies
+      const bool incl = slot < k;
+      const int nxt = __shfl_sync(FULL, e, (k - 1) * G);
+      const int mcn = lane < y1 - nxt ? ld_stream(a.col + nxt + lane) : 0;
+      const float mvn = lane < y1 - nxt ? ld_val(a.val, nxt + lane) : 0.0f;
+      const int mylen = incl ? len : 0;
+      const int maxlen = (int)__reduce_max_sync(FULL, (unsigned)mylen);
+      const int off = sbeg - cstart;
+      zero<V>(acc);
+      for (int k0 = 0; k0 < maxlen; k0 += UL) {
+        typename D::raw_t b[UL];
+        float vv[UL];
+#pragma unroll
+        for (int u = 0; u < UL; ++u) {
+          const bool okk = k0 + u < mylen;
+          const int t = okk ? off + k0 + u : 0;
           const int j = __shfl_sync(FULL, mc, t);
-          vv[u] = __shfl_sync(FULL, mv, t);
+          const float v = __shfl_sync(FULL, mv, t);
+          vv[u] = okk ? v : 0.0f;
           b[u] = D::load(Bc + (size_t)(unsigned)j * ldb, pol);
         }
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-#pragma unroll
-          for (int v = 0; v < V; ++v) acc[v] = fmaf(vv[u], D::get(b[u], v), acc[v]);
-        }
-      }
-      nb = nbn;
-      mc = mcn;
-      mv = mvn;
-      continue;
-    }
-#pragma unroll
-    for (int s0 = 0; s0 < S; s0 += U) {
-      if (s0 * P >= nb) break;
-      typename D::raw_t b[U];
-      float vv[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        // Slots past the batch get j = 0, v = 0: a harmless load of B row 0.
-        const int t = (s0 + u) * P + slot;
-        const int j = __shfl_sync(FULL, mc, t);
-        vv[u] = __shfl_sync(FULL, mv, t);
-        b[u] = D::load(Bc + (size_t)(unsigned)j * ldb, pol);
-      }
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int s = s0 + u;
-        if (s * P >= nb) break;
-        const int qf = p + s * P;                                   // first nonzero of the step
-        const int ql = qf + (nb - s * P < P ? nb - s * P : P) - 1;  // last one
-        if (ql < cend) {
-          if (qf + slot <= ql) {  // slots past the batch hold row 0 of B: skip them
+        for (int u = 0; u < UL; ++u) {
+          if (k0 + u < mylen) {
 #pragma unroll
             for (int v = 0; v < V; ++v) acc[v] = fmaf(vv[u], D::get(b[u], v), acc[v]);
           }
-        } else {
-          // The step reaches the end of row `cur` (and maybe of later rows).
-          const int q = qf + slot;
-          bool pending = q <= ql;
-          for (;;) {
-            if (pending && q < cend) {
-#pragma unroll
-              for (int v = 0; v < V; ++v) acc[v] = fmaf(vv[u], D::get(b[u], v), acc[v]);
-              pending = false;
-            }
-            if (cend > ql) break;
-            flush();
-          }
         }
       }
-    }
-    nb = nbn;
-    mc = mcn;
-    mv = mvn;
-  }
-  // Rows that end after the last nonzero of the unit (or hold none of it).
-  while (cur < x1) flush();
-  if (!ROWS && cur < M) {
-    // Row x1 continues into the next chunk: its partial sum goes out by reduction.
-    const int start = __ldg(a.row_ptr + cur);
-    if (y1 > (start > y0 ? start : y0)) {
-      fold_slots<G, V>(acc);
-      if (slot == 0 && active) atomic_add_c<V>(a.C + (long long)cur * a.ldc + col0, acc);
+      if (incl && active) {
+        float *dst = a.C + (long long)r * a.ldc + col0;
+        if (!ROWS && ((r == x0 && head_split) || (r == x1 && tail_open))) {
+          if (mylen > 0) atomic_add_c<V>(dst, acc);
+        } else {
+          store_c<V>(dst, acc);
+        }
+      }
+      cur += k;
+      cstart = nxt;
+      mc = mcn;
+      mv = mvn;
     }
   }
 }
