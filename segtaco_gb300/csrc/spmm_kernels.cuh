@@ -203,9 +203,12 @@ __global__ void __launch_bounds__(kCta, V == 8 ? 3 : 4) spmm_seg_kernel(SpmmArgs
       ++cur;
     } else {
       // ---- short rows: slot s takes row cur + s -------------------------
+      // Every lane takes part in every shuffle (r - wb <= 31 by the window rule).
       const int r = cur + slot;
-      const int e = r <= last ? min(__shfl_sync(FULL, rw, r - wb), y1) : INT_MAX;
-      const int prev_end = min(__shfl_sync(FULL, rw, r - wb - 1 >= 0 ? r - wb - 1 : 0), y1);
+      const int rw_r = __shfl_sync(FULL, rw, r - wb);
+      const int rw_prev = __shfl_sync(FULL, rw, r - wb - 1 >= 0 ? r - wb - 1 : 0);
+      const int e = r <= last ? min(rw_r, y1) : INT_MAX;
+      const int prev_end = min(rw_prev, y1);
       const int sbeg = slot == 0 ? cstart : prev_end;
       const int len = e - sbeg;
       // Take the longest prefix of slots whose rows are short and fit the batch.
@@ -214,7 +217,8 @@ __global__ void __launch_bounds__(kCta, V == 8 ? 3 : 4) spmm_seg_kernel(SpmmArgs
 #pragma unroll
       for (int q = 0; q < P; ++q) leaders |= 1u << (q * G);
       const unsigned bad = ~__ballot_sync(FULL, ok) & leaders;
-      const int k = bad ? (__ffs(bad) - 1) / G : P;  // >= 1: slot 0 always qualifies
+      int k = bad ? (__ffs(bad) - 1) / G : P;  // slot 0 always qualifies ...
+      if (k < 1) k = 1;                        // ... and the walk must advance regardless
       const bool incl = slot < k;
       const int nxt = __shfl_sync(FULL, e, (k - 1) * G);
       const int mcn = lane < y1 - nxt ? ld_stream(a.col + nxt + lane) : 0;
