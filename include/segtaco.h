@@ -89,6 +89,23 @@ int segtaco_spmm(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr, cons
                  int64_t ldc, int32_t N, const segtaco_config *cfg, void *workspace,
                  size_t workspace_bytes, void *stream);
 
+/* segtaco_spmm without any allocation (no counterpart in segTACO).  For
+ * callers that cannot call cudaMalloc -- a host framework whose allocator
+ * owns the device memory, a serving loop with a memory budget fixed at
+ * start-up, a caller that cannot take an allocation's device-wide sync -- the
+ * element-balanced schedules' scratch (merge-path chunk coordinates) comes
+ * from a fixed 2 MiB array in the library's device memory instead of a
+ * workspace.  Limit: at most 262,143 merge-path chunks, i.e.
+ * ceil((M + nnz) / items_per_unit) <= 262,143 (M + nnz <= ~134M at the default
+ * 512 items); larger problems get SEGTACO_EINVAL.  The first call on each
+ * device looks up the array's address (cudaGetSymbolAddress) and should come
+ * before any stream capture.  All calls share the array: calls that overlap on
+ * the GPU race on it.  SEGTACO_FLAG_PARTITION_READY is not accepted. */
+int segtaco_spmm_noalloc(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr,
+                         const int32_t *col, const float *vals, const void *B, int32_t b_dtype,
+                         int64_t ldb, float *C, int64_t ldc, int32_t N,
+                         const segtaco_config *cfg, void *stream);
+
 /* The first half of segtaco_spmm, for callers that time or overlap it: the
  * merge-path partition of A into `workspace` (element-balanced schedules) and
  * the zeroing of the C rows that straddle chunk edges.  A following

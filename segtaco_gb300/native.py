@@ -77,6 +77,8 @@ SIGNATURES = {
                                               C.POINTER(_SZ)]),
     "segtaco_spmm": (C.c_int, [_I, _I, _I64, _P, _P, _P, _P, _I, _I64, _P, _I64, _I,
                                C.POINTER(Config), _P, _SZ, _P]),
+    "segtaco_spmm_noalloc": (C.c_int, [_I, _I, _I64, _P, _P, _P, _P, _I, _I64, _P, _I64, _I,
+                                       C.POINTER(Config), _P]),
     "segtaco_spmm_partition": (C.c_int, [_I, _I, _I64, _P, _P, _I64, _I, _I, C.POINTER(Config),
                                          _P, _SZ, _P]),
     "segtaco_block_starts_taco": (C.c_int, [_I, _I64, _P, _I, _P, _P]),

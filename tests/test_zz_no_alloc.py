@@ -1,0 +1,58 @@
+"""segtaco_spmm_noalloc: the SpMM entry point that allocates nothing.
+
+It exists for callers that cannot call cudaMalloc (a framework whose own
+allocator owns the device memory, a serving loop whose memory budget is fixed
+at start-up): its scratch is a fixed array inside libsegtaco.  This file is
+collected last so that a run stopping at the first failure has run every other
+test first; it also passes alone in a fresh process.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from gpu_util import TOL, assert_spmm_close, dev, spmm_ref
+from segtaco_gb300 import native as N
+from segtaco_gb300 import ops, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _noalloc(Ad, Bd, Cd, cfg):
+    p = lambda t: None if t is None else C.c_void_p(t.data_ptr())
+    st = N.lib().segtaco_spmm_noalloc(Ad.M, Ad.K, Ad.nnz, p(Ad.row_ptr), p(Ad.col), p(Ad.val),
+                                      p(Bd), N.F32, Bd.stride(0), p(Cd), Cd.stride(0),
+                                      int(Bd.shape[1]), C.byref(cfg),
+                                      C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    return st
+
+
+@pytest.mark.parametrize("sched", ["eb_pr", "eb_sr"])
+def test_noalloc_matches_spmm_twice(cuda, sched):
+    A = synth.power_law(20000, 18000, 1.8, 5000, 0.02, seed=31)
+    B = synth.dense(A.K, 64, seed=32)
+    Ad, Bd = dev(A), torch.from_numpy(B).cuda()
+    cfg = N.Config.make(schedule=sched, items_per_unit=256)
+    ref_c = ops.spmm(Ad, Bd, config=cfg).cpu().numpy()  # the existing entry point
+    ref = spmm_ref(A, B)
+    for _ in range(2):  # the shared scratch keeps the previous call's contents
+        Cd = torch.full((A.M, 64), float("nan"), device="cuda")
+        assert _noalloc(Ad, Bd, Cd, cfg) == N.OK, N.last_error()
+        torch.cuda.synchronize()
+        got = Cd.cpu().numpy()
+        assert_spmm_close(got, A, B, ref=ref)
+        S = ref[1]
+        assert np.all(np.abs(got - ref_c) <= 2 * TOL * np.maximum(S, 1e-30))
+
+
+def test_noalloc_rejects_problems_beyond_its_scratch(cuda):
+    A = synth.power_law(20000, 18000, 1.8, 5000, 0.02, seed=33)
+    Ad = dev(A)
+    Bd = torch.zeros((A.K, 8), device="cuda")
+    Cd = torch.zeros((A.M, 8), device="cuda")
+    cfg = N.Config.make(schedule="eb_pr", items_per_unit=1)  # one chunk per item
+    if A.M + A.nnz + 1 <= 262143:
+        pytest.skip("matrix too small to overflow the fixed scratch")
+    st = _noalloc(Ad, Bd, Cd, cfg)
+    assert st == N.EINVAL and "fixed scratch" in N.last_error()
