@@ -58,6 +58,7 @@ extern "C" {
 #define SEGTACO_FLAG_L2_HINTS 1u  /* gathered B rows evict_last in L2               */
 #define SEGTACO_FLAG_PARTITION_READY 2u /* workspace holds segtaco_spmm_partition()'s
                                            output for this A, C, N and config: skip it */
+#define SEGTACO_FLAG_NO_TMA 4u    /* gather B with register loads, not TMA bulk copies */
 
 /* Tuning knobs.  Zero in a field means "choose automatically". */
 typedef struct segtaco_config {
@@ -71,6 +72,10 @@ typedef struct segtaco_config {
 
 /* Library identity and build checks. */
 const char *segtaco_version(void);
+/* Status word of the device kernels on the current device: SEGTACO_OK, or
+ * SEGTACO_ETIMEOUT if a kernel gave up a bounded wait (its output is then
+ * incomplete).  clear != 0 resets it.  Synchronises the device. */
+int segtaco_device_status(int clear);
 /* Human-readable text of the last error raised on this host thread. */
 const char *segtaco_last_error(void);
 /* 1 when a CUDA device is usable by this process, else 0 (never fails). */

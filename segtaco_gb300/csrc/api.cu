@@ -112,6 +112,9 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
   plan->W = W;
   plan->slabs = (N + W - 1) / W;
   plan->l2_hints = (c.flags & SEGTACO_FLAG_L2_HINTS) != 0;
+  // TMA bulk copies need 16-byte lane vectors and 16-byte aligned segments
+  // (V == 16/esz already implies N, ldb and B are multiples / aligned).
+  plan->use_tma = !(c.flags & SEGTACO_FLAG_NO_TMA) && V * esz == 16;
   plan->rows_per_unit = c.rows_per_unit > 0 ? c.rows_per_unit : 1;
   plan->items_per_unit = 0;
   plan->nchunks = (M + plan->rows_per_unit - 1) / plan->rows_per_unit;  // rb: row blocks
@@ -155,16 +158,19 @@ int run_spmm_planned(const SpmmPlan &plan, int M, int K, long long nnz, const in
   L.part_y = py;
   L.units = plan.nchunks;
   L.rows_per_unit = (int)plan.rows_per_unit;
+  L.use_tma = plan.use_tma;
   const bool bf16 = b_dtype == SEGTACO_BF16;
   switch (plan.schedule) {
     case SEGTACO_RB_SR:
     case SEGTACO_RB_PR:
+      if (L.use_tma) return bf16 ? launch_spmm_tma_bf16(L, true, s) : launch_spmm_tma_f32(L, true, s);
       return bf16 ? launch_spmm_bf16_rows(L, s) : launch_spmm_f32_rows(L, s);
     case SEGTACO_EB_SR:
     case SEGTACO_EB_PR:
       if (!partition_ready)
         SEGTACO_TRY(launch_merge_path(row_ptr, M, nnz, plan.items_per_unit, plan.nchunks, px, py,
                                       C, ldc, N, s));
+      if (L.use_tma) return bf16 ? launch_spmm_tma_bf16(L, false, s) : launch_spmm_tma_f32(L, false, s);
       return bf16 ? launch_spmm_bf16_chunks(L, s) : launch_spmm_f32_chunks(L, s);
     default:
       return set_error(SEGTACO_EINVAL, "unknown schedule %d", plan.schedule);

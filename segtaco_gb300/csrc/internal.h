@@ -71,12 +71,18 @@ struct SpmmLaunch {
   const int *part_x, *part_y;  // chunks only
   long long units;             // warps: merge-path chunks or row blocks
   int rows_per_unit;           // row blocks only
+  bool use_tma;                // gather B with TMA bulk copies (spmm_tma.cuh)
 };
 // One launcher per (dense type, unit kind); each switches over (V, G).
 int launch_spmm_f32_rows(const SpmmLaunch &L, cudaStream_t s);
 int launch_spmm_f32_chunks(const SpmmLaunch &L, cudaStream_t s);
 int launch_spmm_bf16_rows(const SpmmLaunch &L, cudaStream_t s);
 int launch_spmm_bf16_chunks(const SpmmLaunch &L, cudaStream_t s);
+// TMA variants: 16-byte lane vectors only (fp32 x 4, bf16 x 8), any G.
+int launch_spmm_tma_f32(const SpmmLaunch &L, bool rows, cudaStream_t s);
+int launch_spmm_tma_bf16(const SpmmLaunch &L, bool rows, cudaStream_t s);
+// Device status word of the TMA kernels on the current device.
+int tma_status_ptr(int **out);
 
 // Resolved plan of one SpMM call (api.cu).
 struct SpmmPlan {
@@ -85,6 +91,7 @@ struct SpmmPlan {
   long long items_per_unit;  // eb (merge-path D)
   long long nchunks;         // eb
   bool l2_hints;
+  bool use_tma;
   size_t workspace;          // bytes
 };
 int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, long long ldc,

@@ -33,6 +33,7 @@ BF16 = 1
 
 FLAG_L2_HINTS = 1
 FLAG_PARTITION_READY = 2
+FLAG_NO_TMA = 4
 
 
 class SegtacoError(RuntimeError):
@@ -72,6 +73,7 @@ SIGNATURES = {
     "segtaco_version": (C.c_char_p, []),
     "segtaco_last_error": (C.c_char_p, []),
     "segtaco_device_available": (C.c_int, []),
+    "segtaco_device_status": (C.c_int, [C.c_int]),
     "segtaco_autotune_heuristic": (C.c_int, [_I, _I, _I64, _I, _I, _I64, C.POINTER(Config)]),
     "segtaco_spmm_workspace_size": (C.c_int, [_I, _I, _I64, _I, _I, C.POINTER(Config),
                                               C.POINTER(_SZ)]),

@@ -13,6 +13,7 @@ from segtaco_gb300 import ops, synth
 
 pytestmark = pytest.mark.gpu
 SCHEDULES = ["rb_sr", "rb_pr", "eb_sr", "eb_pr"]
+PATHS = {"tma": 0, "regs": N.FLAG_NO_TMA}  # B gathered by TMA bulk copies / register loads
 SMALL = small_cases()
 
 
@@ -24,12 +25,13 @@ def run(A, B, cfg=None, **kw):
     return C.cpu().numpy()
 
 
+@pytest.mark.parametrize("path", list(PATHS))
 @pytest.mark.parametrize("sched", SCHEDULES)
 @pytest.mark.parametrize("name", golden_cases("spmm_"))
-def test_golden(cuda, sched, name):
+def test_golden(cuda, sched, name, path):
     d = load_golden("spmm_", name)
     A = synth.CSR(d["row_ptr"], d["col"], d["val"], int(d["M"]), int(d["K"]))
-    C = run(A, d["B"], N.Config.make(schedule=sched))
+    C = run(A, d["B"], N.Config.make(schedule=sched, flags=PATHS[path]))
     r, S = spmm_ref(A, d["B"])
     if r.size:
         assert O.max_bound_err(C, r, S) <= TOL
@@ -37,13 +39,14 @@ def test_golden(cuda, sched, name):
         assert O.max_bound_err(C, d["C_eigen"].astype(np.float64), S) <= 2 * TOL
 
 
+@pytest.mark.parametrize("path", list(PATHS))
 @pytest.mark.parametrize("sched", SCHEDULES)
 @pytest.mark.parametrize("name", list(SMALL))
-def test_small_cases(cuda, sched, name):
+def test_small_cases(cuda, sched, name, path):
     A = SMALL[name]
-    for n in (1, 4, 33, 128):
+    for n in (1, 4, 8, 33, 64, 128):
         B = synth.dense(A.K, n, seed=n)
-        assert_spmm_close(run(A, B, N.Config.make(schedule=sched)), A, B)
+        assert_spmm_close(run(A, B, N.Config.make(schedule=sched, flags=PATHS[path])), A, B)
 
 
 @pytest.mark.parametrize("sched", SCHEDULES)
@@ -60,9 +63,9 @@ def test_tuning_knobs(cuda, sched):
     B = synth.dense(A.K, 64, seed=5)
     ref = spmm_ref(A, B)
     for col_tile in (4, 16, 32, 64, 128):
-        for vec in (1, 2, 4):
+        for vec, flags in ((1, 0), (2, 0), (4, 0), (4, N.FLAG_NO_TMA)):
             for units in (1, 3, 7, 64, 1024):
-                kw = dict(schedule=sched, col_tile=col_tile, vec=vec)
+                kw = dict(schedule=sched, col_tile=col_tile, vec=vec, flags=flags)
                 if sched.startswith("rb"):
                     if units > 8:
                         continue
@@ -81,13 +84,14 @@ def test_l2_hint_flag(cuda, sched):
     assert_spmm_close(C, A, B)
 
 
-def test_rb_sr_is_the_sequential_fma_order(cuda):
+@pytest.mark.parametrize("path", list(PATHS))
+def test_rb_sr_is_the_sequential_fma_order(cuda, path):
     """rb_sr sums each row in storage order with fmaf: bit-exact with the
     sequential FP32 restatement of Eigen's order using fused multiply-adds."""
     for name in ("powerlaw", "uniform16", "one_long_row"):
         A = SMALL[name]
         B = synth.dense(A.K, 32, seed=7)
-        C = run(A, B, N.Config.make(schedule="rb_sr"))
+        C = run(A, B, N.Config.make(schedule="rb_sr", flags=PATHS[path]))
         assert np.array_equal(C, O.spmm_f32_rowseq(A.row_ptr, A.col, A.val, B, fma=True))
 
 
@@ -116,15 +120,17 @@ def test_strided_and_offset_operands(cuda, sched):
     assert torch.all(Cbig[:, :3] == 7.0)  # columns outside C untouched
 
 
+@pytest.mark.parametrize("path", list(PATHS))
 @pytest.mark.parametrize("sched", SCHEDULES)
-def test_bf16_dense_operand(cuda, sched):
+def test_bf16_dense_operand(cuda, sched, path):
     """bf16 B with fp32 accumulation: within TOL of the exact product with the
     bf16 values; the error against the fp32 B is the bf16 rounding (stated)."""
     A = SMALL["powerlaw"]
     for n in (8, 64, 128, 3):
         B32 = synth.dense(A.K, n, seed=10 + n)
         bits = synth.to_bf16_bits(B32)
-        C = ops.spmm(dev(A), to_torch_bf16(bits), config=N.Config.make(schedule=sched))
+        C = ops.spmm(dev(A), to_torch_bf16(bits),
+                     config=N.Config.make(schedule=sched, flags=PATHS[path]))
         torch.cuda.synchronize()
         C = C.cpu().numpy()
         assert_spmm_close(C, A, bits, bf16=True)
@@ -198,10 +204,16 @@ def test_full_power_law_all_schedules(cuda):
     y = np.bincount(rows_all, weights=A.val.astype(np.float64) * b1[A.col], minlength=A.M)
     yb = np.bincount(rows_all, weights=np.abs(A.val.astype(np.float64)) * b1abs[A.col], minlength=A.M)
     for sched in SCHEDULES:
-        C.fill_(float("nan"))
-        ops.spmm(Ad, Bd, C_out=C, config=N.Config.make(schedule=sched))
-        torch.cuda.synchronize()
-        rs = C.double().sum(dim=1).cpu().numpy()
-        assert np.all(np.abs(rs - y) <= 2 * TOL * np.maximum(yb, 1e-30)), sched
-        got = C[torch.from_numpy(rows).cuda()].cpu().numpy()
-        assert_spmm_close(got, sub, B, ref=ref)
+        for path, flags in PATHS.items():
+            C.fill_(float("nan"))
+            ops.spmm(Ad, Bd, C_out=C, config=N.Config.make(schedule=sched, flags=flags))
+            torch.cuda.synchronize()
+            rs = C.double().sum(dim=1).cpu().numpy()
+            assert np.all(np.abs(rs - y) <= 2 * TOL * np.maximum(yb, 1e-30)), (sched, path)
+            got = C[torch.from_numpy(rows).cuda()].cpu().numpy()
+            assert_spmm_close(got, sub, B, ref=ref)
+
+
+def test_device_status_clean(cuda):
+    """No kernel gave up a bounded wait in this session."""
+    assert N.lib().segtaco_device_status(1) == N.OK
