@@ -71,7 +71,8 @@ struct SpmmLaunch {
   const int *part_x, *part_y;  // chunks only
   long long units;             // warps: merge-path chunks or row blocks
   int rows_per_unit;           // row blocks only
-  bool use_tma;                // gather B with TMA bulk copies (spmm_tma.cuh)
+  bool use_tma;                // gather B into a shared-memory ring (spmm_tma.cuh)
+  bool bulk_copies;            // ... with cp.async.bulk (TMA) rather than cp.async
 };
 // One launcher per (dense type, unit kind); each switches over (V, G).
 int launch_spmm_f32_rows(const SpmmLaunch &L, cudaStream_t s);
@@ -92,6 +93,7 @@ struct SpmmPlan {
   long long nchunks;         // eb
   bool l2_hints;
   bool use_tma;
+  bool bulk_copies;
   size_t workspace;          // bytes
 };
 int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, long long ldc,

@@ -5,13 +5,19 @@
 // lanes form P = 32/G slots; long rows are split over the slots, runs of short
 // rows go one row per slot.  What differs is how the B row segments arrive:
 //
-//   * Producer.  The unit's nonzeros are cut into rounds of 32 positions.  For
-//     a round, lane l issues one cp.async.bulk (TMA) copy of the W-column
-//     segment of B row col[q0+l] into slot l of a per-warp shared-memory ring
-//     of RR rounds; lane 0 first arms that round's mbarrier with the round's
-//     byte count (mbarrier.arrive.expect_tx), and the copies complete on it.
+//   * Producer.  The unit's nonzeros are cut into rounds of 32 positions; the
+//     W-column segment of B row col[q] lands in slot (q - y0) mod 32*RR of a
+//     per-warp shared-memory ring of RR rounds.  Two copy engines:
+//       BULK = true : lane l issues one cp.async.bulk (TMA) copy of segment l;
+//                     lane 0 arms the round's mbarrier with the byte count
+//                     (mbarrier.arrive.expect_tx) and the copies complete on it;
+//       BULK = false: the lanes issue the round's 32*G 16-byte pieces as
+//                     cp.async.cg copies (G each) and every lane arrives on the
+//                     round's mbarrier when its copies have landed
+//                     (cp.async.mbarrier.arrive.noinc).
 //     Up to RR rounds (RR*32 segments) are in flight per warp, none of them in
-//     registers.
+//     registers.  Small bulk copies are limited by the TMA request rate, so the
+//     cp.async engine is the default for these 64-512 byte segments.
 //   * Consumer.  Before it reads nonzero q the warp waits (mbarrier
 //     try_wait.parity) for q's round; then each lane reads its V columns of the
 //     segment with one ld.shared.v4 and does V multiply-adds.  A round's ring
@@ -67,6 +73,16 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t
       "l"(src), "r"(bytes), "r"(bar), "l"(pol)
       : "memory");
 }
+// 16-byte asynchronous copy global -> shared through the load/store unit.
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src, uint64_t pol) {
+  asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(dst),
+               "l"(src), "l"(pol)
+               : "memory");
+}
+// Arrive on `bar` once all of this thread's earlier cp.async copies have landed.
+__device__ __forceinline__ void cp_async_arrive(uint32_t bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
+}
 __device__ __forceinline__ void fence_proxy_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
@@ -104,7 +120,7 @@ template <typename BT, int G, int RR> constexpr int tma_smem_bytes() {
 // window of the walk can straddle two rounds).
 template <int G> constexpr int tma_ring_rounds() { return 32 / G >= 2 ? 32 / G : 2; }
 
-template <typename BT, int G, bool ROWS, int RR>
+template <typename BT, int G, bool ROWS, int RR, bool BULK>
 __global__ void __launch_bounds__(kTmaWarps * 32)
     spmm_tma_kernel(SpmmArgs<BT> a, TmaExtra ex) {
   static_assert(RR >= 2, "a window can straddle two rounds");
@@ -155,7 +171,7 @@ __global__ void __launch_bounds__(kTmaWarps * 32)
 
   if (lane == 0) {
 #pragma unroll
-    for (int b = 0; b < RR; ++b) mbar_init(smem_u32(&bars[b]), 1);
+    for (int b = 0; b < RR; ++b) mbar_init(smem_u32(&bars[b]), BULK ? 1 : 32);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncwarp();
@@ -178,11 +194,26 @@ __global__ void __launch_bounds__(kTmaWarps * 32)
     const int j = pj;
     __syncwarp();
     fence_proxy_async_smem();  // earlier reads of this ring slot before the async writes
-    if (lane == 0) mbar_expect_tx(bar, (uint32_t)n * seg_bytes);
-    __syncwarp();
-    if (lane < n)
-      bulk_g2s(smem_u32(ring + rs * ROUND + lane * SEG), Bs + (size_t)(unsigned)j * ldb,
-               seg_bytes, bar, pol);
+    if (BULK) {
+      if (lane == 0) mbar_expect_tx(bar, (uint32_t)n * seg_bytes);
+      __syncwarp();
+      if (lane < n)
+        bulk_g2s(smem_u32(ring + rs * ROUND + lane * SEG), Bs + (size_t)(unsigned)j * ldb,
+                 seg_bytes, bar, pol);
+    } else {
+      // Lane l copies 16-byte piece c = l % G of positions l/G, l/G + P, ...
+      const int c = lane & (G - 1);
+      const bool piece_ok = (uint32_t)c * 16u < seg_bytes;  // last slab may be narrower
+      const uint32_t dst0 = smem_u32(ring + rs * ROUND + c * 16);
+#pragma unroll
+      for (int k = 0; k < G; ++k) {
+        const int i = lane / G + k * P;
+        const int ji = __shfl_sync(FULL, j, i);
+        if (i < n && piece_ok)
+          cp_async16(dst0 + i * SEG, Bs + (size_t)(unsigned)ji * ldb + c * (16 / sizeof(BT)), pol);
+      }
+      cp_async_arrive(bar);
+    }
     if (rnd + 1 < rounds) load_cols(rnd + 1);
   };
   int waited = 0;  // rounds known complete

@@ -7,11 +7,11 @@
 
 namespace segtaco {
 
-template <typename BT, int G, bool ROWS>
+template <typename BT, int G, bool ROWS, bool BULK>
 int launch_tma_variant(const SpmmLaunch &L, cudaStream_t s) {
   constexpr int RR = tma_ring_rounds<G>();
   constexpr int smem = tma_smem_bytes<BT, G, RR>();
-  auto kern = spmm_tma_kernel<BT, G, ROWS, RR>;
+  auto kern = spmm_tma_kernel<BT, G, ROWS, RR, BULK>;
   static bool configured = false;  // one attribute call per variant and process
   if (!configured) {
     SEGTACO_TRY(check_cuda(
@@ -30,12 +30,16 @@ int launch_tma_variant(const SpmmLaunch &L, cudaStream_t s) {
 }
 
 template <typename BT> int launch_tma(const SpmmLaunch &L, bool rows, cudaStream_t s) {
-  switch (L.G * 2 + (rows ? 1 : 0)) {
+  switch (L.G * 4 + (rows ? 2 : 0) + (L.bulk_copies ? 1 : 0)) {
 #define SEGTACO_TMA_CASE(G)                                  \
-  case G * 2 + 1:                                            \
-    return launch_tma_variant<BT, G, true>(L, s);            \
-  case G * 2:                                                \
-    return launch_tma_variant<BT, G, false>(L, s);
+  case G * 4 + 3:                                            \
+    return launch_tma_variant<BT, G, true, true>(L, s);      \
+  case G * 4 + 2:                                            \
+    return launch_tma_variant<BT, G, true, false>(L, s);     \
+  case G * 4 + 1:                                            \
+    return launch_tma_variant<BT, G, false, true>(L, s);     \
+  case G * 4:                                                \
+    return launch_tma_variant<BT, G, false, false>(L, s);
     SEGTACO_TMA_CASE(1)
     SEGTACO_TMA_CASE(2)
     SEGTACO_TMA_CASE(4)

@@ -34,6 +34,7 @@ BF16 = 1
 FLAG_L2_HINTS = 1
 FLAG_PARTITION_READY = 2
 FLAG_NO_TMA = 4
+FLAG_TMA_BULK = 8
 
 
 class SegtacoError(RuntimeError):

@@ -13,7 +13,9 @@ from segtaco_gb300 import ops, synth
 
 pytestmark = pytest.mark.gpu
 SCHEDULES = ["rb_sr", "rb_pr", "eb_sr", "eb_pr"]
-PATHS = {"tma": 0, "regs": N.FLAG_NO_TMA}  # B gathered by TMA bulk copies / register loads
+# How B rows are gathered: cp.async into a shared-memory ring (default), TMA
+# bulk copies into the ring, or register loads.
+PATHS = {"async": 0, "bulk": N.FLAG_TMA_BULK, "regs": N.FLAG_NO_TMA}
 SMALL = small_cases()
 
 
