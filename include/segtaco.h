@@ -70,6 +70,7 @@ typedef struct segtaco_config {
   int32_t rows_per_unit;  /* rb: rows handled by one lane group / warp            */
   int32_t items_per_unit; /* eb: merge-path items (rows + nonzeros) per unit      */
   uint32_t flags;         /* SEGTACO_FLAG_*                                        */
+  int32_t depth;          /* dense loads in flight per lane (0 = automatic, 4 or 8) */
 } segtaco_config;
 
 /* Library identity and build checks. */

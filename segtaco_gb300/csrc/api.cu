@@ -116,6 +116,9 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
   // (V == 16/esz already implies N, ldb and B are multiples / aligned).
   plan->use_tma = !(c.flags & SEGTACO_FLAG_NO_TMA) && V * esz == 16;
   plan->bulk_copies = (c.flags & SEGTACO_FLAG_TMA_BULK) != 0;
+  if (c.depth != 0 && c.depth != 4 && c.depth != 8)
+    return set_error(SEGTACO_EINVAL, "depth=%d not in {0, 4, 8}", c.depth);
+  plan->deep = c.depth == 8;
   plan->rows_per_unit = c.rows_per_unit > 0 ? c.rows_per_unit : 1;
   plan->items_per_unit = 0;
   plan->nchunks = (M + plan->rows_per_unit - 1) / plan->rows_per_unit;  // rb: row blocks
@@ -161,6 +164,7 @@ int run_spmm_planned(const SpmmPlan &plan, int M, int K, long long nnz, const in
   L.rows_per_unit = (int)plan.rows_per_unit;
   L.use_tma = plan.use_tma;
   L.bulk_copies = plan.bulk_copies;
+  L.deep = plan.deep;
   const bool bf16 = b_dtype == SEGTACO_BF16;
   switch (plan.schedule) {
     case SEGTACO_RB_SR:

@@ -73,6 +73,7 @@ struct SpmmLaunch {
   int rows_per_unit;           // row blocks only
   bool use_tma;                // gather B into a shared-memory ring (spmm_tma.cuh)
   bool bulk_copies;            // ... with cp.async.bulk (TMA) rather than cp.async
+  bool deep;                   // register path: 8 sixteen-byte loads in flight per lane
 };
 // One launcher per (dense type, unit kind); each switches over (V, G).
 int launch_spmm_f32_rows(const SpmmLaunch &L, cudaStream_t s);
@@ -94,6 +95,7 @@ struct SpmmPlan {
   bool l2_hints;
   bool use_tma;
   bool bulk_copies;
+  bool deep;
   size_t workspace;          // bytes
 };
 int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, long long ldc,

@@ -80,16 +80,19 @@ template <int G, int V> __device__ __forceinline__ void fold_slots(float (&r)[V]
   }
 }
 
-// 4 CTAs (32 warps) per SM: at most 64 registers; the bf16 x 8 variants need
-// a few more for their 8 accumulators and run 3 CTAs per SM.
-template <typename BT, int V, int G, bool ROWS>
-__global__ void __launch_bounds__(kCta, V == 8 ? 3 : 4) spmm_seg_kernel(SpmmArgs<BT> a) {
+// DEEP = false: 4 CTAs (32 warps) per SM, at most 64 registers; sixteen-byte
+// vectors keep 4 loads in flight per lane (the bf16 x 8 variants need a few
+// more registers for their 8 accumulators and run 3 CTAs per SM).
+// DEEP = true: 8 loads in flight per lane at 3 CTAs (24 warps) per SM.
+template <typename BT, int V, int G, bool ROWS, bool DEEP = false>
+__global__ void __launch_bounds__(kCta, (V == 8 || DEEP) ? 3 : 4)
+    spmm_seg_kernel(SpmmArgs<BT> a) {
   constexpr int P = 32 / G;                 // slots
   // Rows with >= LONG nonzeros are split over the slots (LONG <= 32, so a
   // short row always fits one batch).
   constexpr int LONG = P == 1 ? 0 : (2 * P < 32 ? 2 * P : 32);
   // B loads in flight per lane: 4 sixteen-byte or 8 narrower raw vectors.
-  constexpr int UL = V * (int)sizeof(BT) >= 16 ? 4 : 8;
+  constexpr int UL = (V * (int)sizeof(BT) >= 16 && !DEEP) ? 4 : 8;
   constexpr int UB = G < UL ? G : UL;       // steps per sub-batch in a split row
   using D = Dense<BT, V>;
   const unsigned FULL = 0xffffffffu;

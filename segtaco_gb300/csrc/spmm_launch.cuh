@@ -48,12 +48,29 @@ inline dim3 spmm_grid(const SpmmLaunch &L) {
 #define SEGTACO_VG_BF16(X, R) \
   SEGTACO_VG_F32(X, R) X(8, 1, R) X(8, 2, R) X(8, 4, R) X(8, 8, R) X(8, 16, R) X(8, 32, R)
 
+// Sixteen-byte-vector variants with 8 loads in flight per lane.
+#define SEGTACO_DEEP_CASE(BT, G, R) \
+  case G:                           \
+    spmm_seg_kernel<BT, 16 / sizeof(BT), G, R, true><<<grid, kCta, 0, s>>>(a); \
+    break;
+#define SEGTACO_DEEP_CASES(BT, R)                                             \
+  SEGTACO_DEEP_CASE(BT, 1, R) SEGTACO_DEEP_CASE(BT, 2, R) SEGTACO_DEEP_CASE(BT, 4, R) \
+  SEGTACO_DEEP_CASE(BT, 8, R) SEGTACO_DEEP_CASE(BT, 16, R) SEGTACO_DEEP_CASE(BT, 32, R)
+
 // Defines int NAME(const SpmmLaunch&, cudaStream_t) for one (dtype, unit kind).
 #define SEGTACO_DEFINE_SPMM_LAUNCHER(NAME, BT, VG_LIST, ROWS)                             \
   namespace segtaco {                                                                     \
   int NAME(const SpmmLaunch &L, cudaStream_t s) {                                         \
     const SpmmArgs<BT> a = make_spmm_args<BT>(L);                                         \
     const dim3 grid = spmm_grid(L);                                                       \
+    if (L.deep && L.V * (int)sizeof(BT) == 16) {                                          \
+      switch (L.G) {                                                                      \
+        SEGTACO_DEEP_CASES(BT, ROWS)                                                      \
+        default:                                                                          \
+          return set_error(SEGTACO_EUNSUPPORTED, #NAME ": no deep variant G=%d", L.G);     \
+      }                                                                                   \
+      return check_launch(#NAME);                                                         \
+    }                                                                                     \
     switch (L.V * 100 + L.G) {                                                            \
       VG_LIST(SEGTACO_SPMM_CASE, ROWS)                                                    \
       default:                                                                            \
