@@ -259,13 +259,15 @@ def run_ours(args, world, rank, local):
     stream = torch.cuda.Stream()
     peak, peak_kind = peak_hbm()
 
-    if args.schedule == "auto":
-        h = N_.Config()
-        N_.check(N_.lib().segtaco_autotune_heuristic(A.M, A.K, A.nnz, N, N_.F32,
-                                                     int(A.row_lengths().max()), h))
-        cfg = h
-    else:
-        cfg = N_.Config.make(schedule=args.schedule)
+    max_len = int(A.row_lengths().max())
+
+    def tuned(schedule):
+        """The library's choice for this shape (schedule -1 = let it pick)."""
+        h = N_.Config.make(schedule=schedule)
+        N_.check(N_.lib().segtaco_autotune_heuristic(A.M, A.K, A.nnz, N, N_.F32, max_len, h))
+        return h
+
+    cfg = tuned(N_.AUTO if args.schedule == "auto" else N_.SCHEDULES[args.schedule])
     if args.col_tile:
         cfg.col_tile = args.col_tile
     if args.items:
@@ -279,11 +281,13 @@ def run_ours(args, world, rank, local):
     schedules = {}
     if args.all_schedules:
         for s in ("rb_sr", "rb_pr", "eb_sr", "eb_pr"):
-            c = N_.Config.make(schedule=s, col_tile=cfg.col_tile, flags=cfg.flags)
+            c = tuned(N_.SCHEDULES[s])
+            c.flags |= cfg.flags & N_.FLAG_L2_HINTS
             wsz = max(256, ops.spmm_workspace_size(Ad, N, N_.F32, c))
             w = torch.empty(wsz, dtype=torch.uint8, device="cuda")
             st, kt = time_spmm(ops, N_, Ad, Bd, Cd, c, w, stream, max(3, args.steps // 2), 2)
-            schedules[s] = {"ms_per_step": round(st, 4), "kernel_ms": round(kt, 4),
+            schedules[s] = {"config": {k: v for k, v in c.as_dict().items() if v},
+                            "ms_per_step": round(st, 4), "kernel_ms": round(kt, 4),
                             "GBps": round(byts / st / 1e6, 1),
                             "roofline_frac": round(byts / kt / 1e6 / peak, 4)}
             del w

@@ -58,9 +58,11 @@ extern "C" {
 #define SEGTACO_FLAG_L2_HINTS 1u  /* gathered B rows evict_last in L2               */
 #define SEGTACO_FLAG_PARTITION_READY 2u /* workspace holds segtaco_spmm_partition()'s
                                            output for this A, C, N and config: skip it */
-#define SEGTACO_FLAG_NO_TMA 4u    /* gather B with register loads, not the async smem ring */
-#define SEGTACO_FLAG_TMA_BULK 8u  /* fill the smem ring with cp.async.bulk (TMA) copies
-                                     rather than 16-byte cp.async copies */
+#define SEGTACO_FLAG_SMEM_RING 4u /* gather B rows into a shared-memory ring with
+                                     cp.async (16-byte vectors only) instead of loading
+                                     them into registers */
+#define SEGTACO_FLAG_TMA_BULK 8u  /* with SMEM_RING: fill the ring with cp.async.bulk
+                                     (TMA) copies rather than 16-byte cp.async copies */
 
 /* Tuning knobs.  Zero in a field means "choose automatically". */
 typedef struct segtaco_config {

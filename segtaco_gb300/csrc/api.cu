@@ -114,7 +114,7 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
   plan->l2_hints = (c.flags & SEGTACO_FLAG_L2_HINTS) != 0;
   // TMA bulk copies need 16-byte lane vectors and 16-byte aligned segments
   // (V == 16/esz already implies N, ldb and B are multiples / aligned).
-  plan->use_tma = !(c.flags & SEGTACO_FLAG_NO_TMA) && V * esz == 16;
+  plan->use_tma = (c.flags & SEGTACO_FLAG_SMEM_RING) && V * esz == 16;
   plan->bulk_copies = (c.flags & SEGTACO_FLAG_TMA_BULK) != 0;
   if (c.depth != 0 && c.depth != 4 && c.depth != 8)
     return set_error(SEGTACO_EINVAL, "depth=%d not in {0, 4, 8}", c.depth);
@@ -219,17 +219,28 @@ int segtaco_device_available(void) {
 int segtaco_autotune_heuristic(int32_t M, int32_t K, int64_t nnz, int32_t N, int32_t b_dtype,
                                int64_t max_row_len, segtaco_config *cfg) {
   if (!cfg) return set_error(SEGTACO_EINVAL, "cfg is NULL");
+  const int requested = cfg->schedule;
   memset(cfg, 0, sizeof(*cfg));
   const double mean = M > 0 ? (double)nnz / M : 0.0;
-  // Row-balanced sequential when rows are short and even; merge path otherwise.
+  // Row-balanced when rows are short and even; merge path otherwise.
   const bool even = max_row_len >= 0 && mean > 0.0 && (double)max_row_len <= 4.0 * mean + 8.0;
-  cfg->schedule = even ? SEGTACO_RB_PR : SEGTACO_EB_PR;
+  const int schedule = (requested >= SEGTACO_RB_SR && requested <= SEGTACO_EB_PR)
+                           ? requested
+                           : (even ? SEGTACO_RB_PR : SEGTACO_EB_PR);
+  cfg->schedule = schedule;
   const int esz = b_dtype == SEGTACO_BF16 ? 2 : 4;
-  // Whole B fits comfortably in L2: one slab as wide as N (up to 128 columns).
+  const bool sequential = schedule == SEGTACO_RB_SR || schedule == SEGTACO_EB_SR;
+  // Column slab: the B slab should stay in L2 (measured on GB300: 128-byte
+  // segments for the parallel schedules; the sequential ones take 16-byte
+  // vectors on all 32 lanes).  A B that fits L2 whole is one slab.
   const double bbytes = (double)K * N * esz;
-  cfg->col_tile = bbytes <= 48e6 ? (N <= 128 ? N : 128) : 128 / esz;
-  cfg->items_per_unit = 256;
-  cfg->rows_per_unit = 1;
+  if (sequential)
+    cfg->col_tile = 32 * (16 / esz);
+  else
+    cfg->col_tile = bbytes <= 48e6 ? (N <= 64 * 4 / esz ? N : 64 * 4 / esz) : 128 / esz;
+  cfg->items_per_unit = 512;
+  cfg->rows_per_unit = schedule == SEGTACO_RB_PR || schedule == SEGTACO_RB_SR ? 4 : 1;
+  cfg->depth = (schedule == SEGTACO_RB_SR || schedule == SEGTACO_RB_PR) ? 8 : 4;
   cfg->flags = 0;
   return SEGTACO_OK;
 }

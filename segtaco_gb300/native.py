@@ -33,7 +33,7 @@ BF16 = 1
 
 FLAG_L2_HINTS = 1
 FLAG_PARTITION_READY = 2
-FLAG_NO_TMA = 4
+FLAG_SMEM_RING = 4
 FLAG_TMA_BULK = 8
 
 

@@ -127,8 +127,10 @@ def test_workspace_and_heuristic(native_lib):
                                          C.byref(out)) == N.OK
     assert out.value == 0
     h = N.Config()
+    h.schedule = -1
     assert L.segtaco_autotune_heuristic(16384, 16384, 262144, 32, N.F32, 16, C.byref(h)) == N.OK
     assert h.schedule == N.RB_PR
+    h.schedule = -1
     assert L.segtaco_autotune_heuristic(10**6, 10**6, 2 * 10**7, 128, N.F32, 48679,
                                         C.byref(h)) == N.OK
     assert h.schedule == N.EB_PR
