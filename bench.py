@@ -292,6 +292,27 @@ def run_ours(args, world, rank, local):
                             "roofline_frac": round(byts / kt / 1e6 / peak, 4)}
             del w
 
+    # cuSPARSE CSR_ALG2 on the same resident operands (segTACO's vendor comparator)
+    vendor = None
+    if not args.no_vendor:
+        try:
+            for _ in range(2):
+                ops.vendor_spmm(Ad, Bd, Cd, stream=stream)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            nv = max(3, args.steps // 2)
+            e0.record(stream)
+            for _ in range(nv):
+                ops.vendor_spmm(Ad, Bd, Cd, stream=stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            vms = e0.elapsed_time(e1) / nv
+            vendor = {"library": "cuSPARSE CSR_ALG2 (row-major)", "ms_per_step": round(vms, 4),
+                      "GBps": round(byts / vms / 1e6, 1),
+                      "note": "includes per-call handle/descriptor setup"}
+        except Exception as exc:  # the comparator is context, not the product
+            vendor = {"error": str(exc)[:200]}
+
     sampler = ClockSampler(local)
     barrier(world)
     torch.cuda.synchronize()
@@ -366,6 +387,7 @@ def run_ours(args, world, rank, local):
                          "kernel_ms": round(kern_ms, 4), "peak_source": peak_kind + " hbm_gbs"},
             "gpu_launches": args.steps * (2 if eb else 1),
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks, "schedules": schedules,
+            "vendor": vendor,
         }
         print(json.dumps(line), flush=True)
 
@@ -385,6 +407,7 @@ def main():
     ap.add_argument("--no-all-schedules", dest="all_schedules", action="store_false")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-vendor", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup(args)

@@ -128,6 +128,46 @@ int segtaco_spmm_partition(int32_t M, int32_t K, int64_t nnz, const int32_t *row
                            const segtaco_config *cfg, void *workspace, size_t workspace_bytes,
                            void *stream);
 
+/* cuSPARSE SpMM (CSR_ALG2, row-major) on the same operands: the vendor
+ * comparator segTACO verifies against (spmm_csr_gpu_cusparse.h:171-260).
+ * Not a hot path; creates and destroys a cuSPARSE handle per call. */
+int segtaco_vendor_spmm(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr,
+                        const int32_t *col, const float *vals, const float *B, int64_t ldb,
+                        float *C, int64_t ldc, int32_t N, void *stream);
+
+/* ---- batched SpMM: many uneven products, one persistent launch per kernel
+ * variant, optionally replayed as a CUDA graph --------------------------- */
+typedef struct segtaco_spmm_problem {
+  int32_t M, K, N, b_dtype;
+  int64_t nnz;
+  const int32_t *row_ptr, *col; /* device CSR of A                      */
+  const float *vals;            /* NULL: all ones                       */
+  const void *B;                /* K x N, row-major, leading dim ldb    */
+  int64_t ldb;
+  float *C;                     /* M x N, row-major, leading dim ldc    */
+  int64_t ldc;
+} segtaco_spmm_problem;
+typedef struct segtaco_batch segtaco_batch;
+/* Plans `count` problems.  configs == NULL: each problem's config comes from
+ * segtaco_autotune_heuristic on its row-length statistics (computed on the
+ * device; the call synchronises `stream`).  The operand pointers are baked
+ * into the batch: later runs compute with whatever the buffers then hold. */
+int segtaco_batch_create(int32_t count, const segtaco_spmm_problem *problems,
+                         const segtaco_config *configs, void *stream, segtaco_batch **out);
+/* Enqueue every product of the batch on `stream`. */
+int segtaco_batch_run(segtaco_batch *batch, void *stream);
+/* Same, through a CUDA graph captured on the first call and replayed after. */
+int segtaco_batch_run_graph(segtaco_batch *batch, void *stream);
+/* Kernel-variant groups, total work items, and (if configs != NULL, count
+ * entries) the configuration chosen for each problem. */
+int segtaco_batch_info(const segtaco_batch *batch, int32_t *groups, int64_t *items,
+                       segtaco_config *configs);
+int segtaco_batch_destroy(segtaco_batch *batch);
+/* Row-length statistics of a device CSR (the autotuner's input):
+ * stats[0] max row length, [1] empty rows, [2] rows >= 32, [3] nonzeros in
+ * rows >= 32.  Synchronises `stream`. */
+int segtaco_row_stats(int32_t M, const int32_t *row_ptr, int64_t *stats, void *stream);
+
 /* ---- partition arrays (exported so they can be checked bit-exactly) ---- */
 /* segTACO's block starts: out[b] = taco_binarySearchBefore(row_ptr, 0, M, b*P)
  * for b = 0..ceil(nnz/P)  (gpu_library.h:185-240).  out has ceil(nnz/P)+1 entries. */

@@ -80,13 +80,11 @@ template <int G, int V> __device__ __forceinline__ void fold_slots(float (&r)[V]
   }
 }
 
-// DEEP = false: 4 CTAs (32 warps) per SM, at most 64 registers; sixteen-byte
-// vectors keep 4 loads in flight per lane (the bf16 x 8 variants need a few
-// more registers for their 8 accumulators and run 3 CTAs per SM).
-// DEEP = true: 8 loads in flight per lane at 3 CTAs (24 warps) per SM.
-template <typename BT, int V, int G, bool ROWS, bool DEEP = false>
-__global__ void __launch_bounds__(kCta, (V == 8 || DEEP) ? 3 : 4)
-    spmm_seg_kernel(SpmmArgs<BT> a) {
+// Walk one unit (merge-path chunk or row block) `w` over column slab `slab`.
+// The body of every SpMM kernel below (single problem or batched).
+template <typename BT, int V, int G, bool ROWS, bool DEEP>
+__device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long w, int slab,
+                                               int lane) {
   constexpr int P = 32 / G;                 // slots
   // Rows with >= LONG nonzeros are split over the slots (LONG <= 32, so a
   // short row always fits one batch).
@@ -96,12 +94,9 @@ __global__ void __launch_bounds__(kCta, (V == 8 || DEEP) ? 3 : 4)
   constexpr int UB = G < UL ? G : UL;       // steps per sub-batch in a split row
   using D = Dense<BT, V>;
   const unsigned FULL = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
   const int slot = lane / G, gl = lane & (G - 1);
-  const long long w = (long long)blockIdx.x * (kCta / 32) + threadIdx.x / 32;
-  if (w >= a.units) return;  // whole warp leaves together
   const int M = a.M;
-  const int col0 = blockIdx.y * (G * V) + gl * V;
+  const int col0 = slab * (G * V) + gl * V;
   const bool active = col0 < a.N;
   const uint64_t pol = l2_policy(a.l2_hints);
   // Inactive lanes (past N) still load, from column 0, so that no address is
@@ -264,6 +259,18 @@ __global__ void __launch_bounds__(kCta, (V == 8 || DEEP) ? 3 : 4)
       mv = mvn;
     }
   }
+}
+
+// DEEP = false: 4 CTAs (32 warps) per SM, at most 64 registers; sixteen-byte
+// vectors keep 4 loads in flight per lane (the bf16 x 8 variants need a few
+// more registers for their 8 accumulators and run 3 CTAs per SM).
+// DEEP = true: 8 loads in flight per lane at 3 CTAs (24 warps) per SM.
+template <typename BT, int V, int G, bool ROWS, bool DEEP = false>
+__global__ void __launch_bounds__(kCta, (V == 8 || DEEP) ? 3 : 4)
+    spmm_seg_kernel(SpmmArgs<BT> a) {
+  const long long w = (long long)blockIdx.x * (kCta / 32) + threadIdx.x / 32;
+  if (w >= a.units) return;  // whole warp leaves together
+  spmm_walk_unit<BT, V, G, ROWS, DEEP>(a, w, blockIdx.y, threadIdx.x & 31);
 }
 
 }  // namespace segtaco

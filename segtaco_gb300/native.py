@@ -60,6 +60,14 @@ class Config(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class SpmmProblem(C.Structure):
+    """segtaco_spmm_problem: one SpMM of a batch (device pointers)."""
+    _fields_ = [("M", C.c_int32), ("K", C.c_int32), ("N", C.c_int32), ("b_dtype", C.c_int32),
+                ("nnz", C.c_int64), ("row_ptr", C.c_void_p), ("col", C.c_void_p),
+                ("vals", C.c_void_p), ("B", C.c_void_p), ("ldb", C.c_int64), ("C", C.c_void_p),
+                ("ldc", C.c_int64)]
+
+
 class TacoTensor(C.Structure):
     """taco_tensor_t (segTACO taco_tensor_t.h:6-15), same layout."""
     _fields_ = [("order", C.c_int32), ("dimensions", C.POINTER(C.c_int32)),
@@ -84,6 +92,14 @@ SIGNATURES = {
                                        C.POINTER(Config), _P]),
     "segtaco_spmm_partition": (C.c_int, [_I, _I, _I64, _P, _P, _I64, _I, _I, C.POINTER(Config),
                                          _P, _SZ, _P]),
+    "segtaco_vendor_spmm": (C.c_int, [_I, _I, _I64, _P, _P, _P, _P, _I64, _P, _I64, _I, _P]),
+    "segtaco_batch_create": (C.c_int, [_I, C.POINTER(SpmmProblem), C.POINTER(Config), _P,
+                                       C.POINTER(_P)]),
+    "segtaco_batch_run": (C.c_int, [_P, _P]),
+    "segtaco_batch_run_graph": (C.c_int, [_P, _P]),
+    "segtaco_batch_info": (C.c_int, [_P, C.POINTER(_I), C.POINTER(_I64), C.POINTER(Config)]),
+    "segtaco_batch_destroy": (C.c_int, [_P]),
+    "segtaco_row_stats": (C.c_int, [_I, _P, C.POINTER(_I64), _P]),
     "segtaco_block_starts_taco": (C.c_int, [_I, _I64, _P, _I, _P, _P]),
     "segtaco_block_starts_canonical": (C.c_int, [_I, _I64, _P, _I, _P, _P]),
     "segtaco_merge_path": (C.c_int, [_I, _I64, _P, _I64, _P, _P, _P]),

@@ -87,6 +87,17 @@ def spmm(A: DeviceCSR, B: torch.Tensor, C_out: torch.Tensor | None = None,
     return C_out
 
 
+def vendor_spmm(A: DeviceCSR, B: torch.Tensor, C_out: torch.Tensor | None = None, stream=None):
+    """cuSPARSE CSR_ALG2 on the same operands (comparator only)."""
+    n = int(B.shape[1])
+    if C_out is None:
+        C_out = torch.empty((A.M, n), dtype=torch.float32, device=B.device)
+    N.check(N.lib().segtaco_vendor_spmm(A.M, A.K, A.nnz, _ptr(A.row_ptr), _ptr(A.col), _ptr(A.val),
+                                        _ptr(B), B.stride(0), _ptr(C_out), C_out.stride(0), n,
+                                        _stream(stream)))
+    return C_out
+
+
 def spmm_partition(A: DeviceCSR, C_out: torch.Tensor, config: N.Config, workspace: torch.Tensor,
                    b_dtype=N.F32, stream=None) -> None:
     """First half of spmm(): partition + zeroing of split rows of C_out; follow
@@ -164,3 +175,60 @@ def csr_validate(A: DeviceCSR, stream=None):
     """Raises SegtacoError(EINVAL) if the device CSR is malformed."""
     N.check(N.lib().segtaco_csr_validate(A.M, A.K, A.nnz, _ptr(A.row_ptr), _ptr(A.col),
                                          _stream(stream)))
+
+
+def row_stats(A: DeviceCSR, stream=None):
+    """Row-length statistics: (max length, empty rows, rows >= 32, nonzeros in rows >= 32)."""
+    out = (C.c_int64 * 4)()
+    N.check(N.lib().segtaco_row_stats(A.M, _ptr(A.row_ptr), out, _stream(stream)))
+    return tuple(out)
+
+
+class Batch:
+    """Many SpMMs planned together and run by one persistent launch per kernel
+    variant (segtaco_batch_*).  `items` is a list of (DeviceCSR, B, C) with B
+    fp32 or bf16 (K x N) and C fp32 (M x N); configs=None autotunes each."""
+
+    def __init__(self, items, configs=None, stream=None):
+        self._keep = list(items)
+        probs = (N.SpmmProblem * len(items))()
+        for p, (A, B, Cm) in zip(probs, items):
+            p.M, p.K, p.N = A.M, A.K, int(B.shape[1])
+            p.b_dtype = _dense_dtype(B)
+            p.nnz = A.nnz
+            p.row_ptr = A.row_ptr.data_ptr()
+            p.col = A.col.data_ptr() if A.nnz else None
+            p.vals = A.val.data_ptr() if A.val is not None else None
+            p.B = B.data_ptr()
+            p.ldb = B.stride(0)
+            p.C = Cm.data_ptr()
+            p.ldc = Cm.stride(0)
+        cfgs = None
+        if configs is not None:
+            cfgs = (N.Config * len(items))(*configs)
+        h = C.c_void_p()
+        N.check(N.lib().segtaco_batch_create(len(items), probs, cfgs, _stream(stream), C.byref(h)))
+        self._h = h
+        self.count = len(items)
+
+    def run(self, stream=None, graph=False):
+        fn = N.lib().segtaco_batch_run_graph if graph else N.lib().segtaco_batch_run
+        N.check(fn(self._h, _stream(stream)))
+
+    def info(self):
+        g = C.c_int32()
+        it = C.c_int64()
+        cfgs = (N.Config * max(1, self.count))()
+        N.check(N.lib().segtaco_batch_info(self._h, C.byref(g), C.byref(it), cfgs))
+        return g.value, it.value, [cfgs[i] for i in range(self.count)]
+
+    def close(self):
+        if self._h:
+            N.lib().segtaco_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -114,6 +114,30 @@ def test_argument_errors_without_device(native_lib):
     assert L.segtaco_taco_call(b"no_such_kernel", None, None, None, None) == N.EINVAL
 
 
+def test_batch_argument_errors_without_device(native_lib):
+    L = native_lib
+    h = C.c_void_p()
+    assert L.segtaco_batch_create(-1, None, None, None, C.byref(h)) == N.EINVAL
+    assert L.segtaco_batch_create(1, None, None, None, C.byref(h)) == N.EINVAL
+    probs = (N.SpmmProblem * 2)()
+    probs[0].M, probs[0].K, probs[0].N, probs[0].nnz = 4, 4, 4, 0
+    probs[0].row_ptr = probs[0].B = probs[0].C = 256
+    probs[0].ldb = probs[0].ldc = 4
+    probs[1] = probs[0]
+    probs[1].ldc = 2  # ldc < N
+    cfgs = (N.Config * 2)(N.Config.make(), N.Config.make())
+    st = L.segtaco_batch_create(2, probs, cfgs, None, C.byref(h))
+    assert st == N.EINVAL and "problem 1" in N.last_error() and not h.value
+    probs[1].ldc, probs[1].b_dtype = 4, 5
+    assert L.segtaco_batch_create(2, probs, cfgs, None, C.byref(h)) == N.EINVAL
+    assert L.segtaco_batch_run(None, None) == N.EINVAL
+    assert L.segtaco_batch_run_graph(None, None) == N.EINVAL
+    assert L.segtaco_batch_info(None, None, None, None) == N.EINVAL
+    assert L.segtaco_batch_destroy(None) == N.OK
+    st = (C.c_int64 * 4)()
+    assert L.segtaco_row_stats(-1, None, st, None) == N.EINVAL
+
+
 def test_workspace_and_heuristic(native_lib):
     L = native_lib
     out = C.c_size_t()

@@ -219,3 +219,13 @@ def test_full_power_law_all_schedules(cuda):
 def test_device_status_clean(cuda):
     """No kernel gave up a bounded wait in this session."""
     assert N.lib().segtaco_device_status(1) == N.OK
+
+
+def test_vendor_comparator_matches_oracle(cuda):
+    """segtaco_vendor_spmm (cuSPARSE CSR SpMM, the comparator the spmm_csr_cusparse
+    names run) computes the same product within the FP32 bound."""
+    A = synth.power_law(3000, 2500, 1.8, 2000, 0.02, seed=21)
+    B = synth.dense(A.K, 40, seed=22)
+    C = ops.vendor_spmm(dev(A), torch.from_numpy(B).cuda())
+    torch.cuda.synchronize()
+    assert_spmm_close(C.cpu().numpy(), A, B)
