@@ -244,6 +244,71 @@ def time_spmm(ops, N_, Ad, Bd, Cd, cfg, ws, stream, steps, warmup):
     return step, kern
 
 
+def run_batched(args, N_, ops, stream, count=256):
+    """Uneven-size stream: `count` pool matrices (M = K log-uniform in [1e3, 2e5],
+    lognormal row lengths of mean 12, four structures, N in {16, 32, 64, 128},
+    FP32).  Per-call launches (one segtaco_spmm per matrix, each with the
+    library's tuned config) against the batched persistent launch, direct and
+    replayed from its CUDA graph."""
+    import numpy as np
+    import torch
+    from segtaco_gb300 import synth
+
+    items, byts, nnz = [], 0, 0
+    for m in range(count):
+        A, n, _ = synth.pool_matrix(m)
+        B = torch.from_numpy(synth.dense(A.K, n, seed=1000 + m)).cuda()
+        C = torch.empty((A.M, n), dtype=torch.float32, device="cuda")
+        items.append((ops.DeviceCSR.from_host(A, "cuda"), B, C))
+        byts += algorithmic_bytes(A.M, A.K, A.nnz, n)
+        nnz += A.nnz
+    batch = ops.Batch(items, stream=stream)
+    groups, nitems, cfgs = batch.info()
+    wsz = max(max(256, ops.spmm_workspace_size(Ad, B.shape[1], N_.F32, c))
+              for (Ad, B, _), c in zip(items, cfgs))
+    ws = torch.empty(wsz, dtype=torch.uint8, device="cuda")
+
+    def per_call():
+        for (Ad, B, C), c in zip(items, cfgs):
+            ops.spmm(Ad, B, C_out=C, config=c, workspace=ws, stream=stream)
+
+    def timed(fn, reps):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    reps = max(3, args.steps // 4)
+    t_call = timed(per_call, reps)
+    t_batch = timed(lambda: batch.run(stream=stream), reps)
+    t_graph = timed(lambda: batch.run(stream=stream, graph=True), reps)
+    launches_call = sum(2 if c.schedule in (N_.EB_SR, N_.EB_PR) else 1 for c in cfgs)
+    batch.close()
+    scheds = {}
+    for c in cfgs:
+        k = {v: k for k, v in N_.SCHEDULES.items()}[c.schedule]
+        scheds[k] = scheds.get(k, 0) + 1
+    return {
+        "workload": "%d uneven matrices, M=K log-uniform [1e3, 2e5], row lengths lognormal "
+                    "mean 12, N in {16,32,64,128}, FP32; %d nnz in all" % (count, nnz),
+        "metric": "SpMMs/s", "per_call_ms": round(t_call, 3), "batched_ms": round(t_batch, 3),
+        "batched_graph_ms": round(t_graph, 3),
+        "per_call_spmms_per_s": round(count / t_call * 1e3, 1),
+        "batched_spmms_per_s": round(count / t_graph * 1e3, 1),
+        "speedup_vs_per_call": round(t_call / t_graph, 3),
+        "batched_GBps": round(byts / t_graph / 1e6, 1),
+        "per_call_launches": launches_call, "batched_launches": groups + 1,
+        "batch_groups": groups, "queue_items": nitems, "schedules": scheds,
+        "timing": "CUDA events on one stream, mean of %d repetitions after 2" % reps,
+    }
+
+
 def run_ours(args, world, rank, local):
     import numpy as np
     import torch
@@ -361,6 +426,10 @@ def run_ours(args, world, rank, local):
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": A.M * N * 4,
                "ms_per_step": round(t_e2e * 1e3, 3), "entry_point": name}
 
+    batched = None
+    if not args.no_batched:
+        batched = run_batched(args, N_, ops, stream)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         sec, Ms, nnzs, threads = cpu_spmm_timed(A, B, 2)
@@ -387,7 +456,7 @@ def run_ours(args, world, rank, local):
                          "kernel_ms": round(kern_ms, 4), "peak_source": peak_kind + " hbm_gbs"},
             "gpu_launches": args.steps * (2 if eb else 1),
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks, "schedules": schedules,
-            "vendor": vendor,
+            "vendor": vendor, "batched": batched,
         }
         print(json.dumps(line), flush=True)
 
@@ -408,6 +477,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-vendor", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup(args)
