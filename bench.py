@@ -309,6 +309,97 @@ def run_batched(args, N_, ops, stream, count=256):
     }
 
 
+def serving_stream(n_req, pool_size=1024, lam=20000.0, recent=8, p_repeat=0.8, seed=0):
+    """Request stream of the serving workload: Poisson arrivals at `lam` per
+    second, op SpMM or SDDMM 50/50, matrix id one of the `recent` most recently
+    used ids with probability p_repeat, else a uniform draw from the pool."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1e6 / lam, size=n_req))
+    is_spmm = rng.random(n_req) < 0.5
+    ids, last = [], []
+    for _ in range(n_req):
+        if last and rng.random() < p_repeat:
+            m = last[int(rng.integers(0, len(last)))]
+        else:
+            m = int(rng.integers(0, pool_size))
+        ids.append(m)
+        if m in last:
+            last.remove(m)
+        last.append(m)
+        del last[:-recent]
+    return arrivals, is_spmm, ids
+
+
+def run_serving(args, N_, n_req=2000, bf16=False):
+    """Served SpMM/SDDMM stream through segtaco_server (continuous batching over
+    a device CSR cache), against the same stream in per-call mode (one request
+    per launch).  Dense operands come from pinned host memory and results go
+    back to pinned host memory, so every request pays its copies."""
+    import numpy as np
+    import torch
+    from segtaco_gb300 import synth
+    from segtaco_gb300.serving import Server
+
+    arrivals, is_spmm, ids = serving_stream(n_req)
+    mats = {m: synth.pool_matrix(m) for m in sorted(set(ids))}
+    maxK = max(A.K for A, _, _ in mats.values())
+    maxM = max(A.M for A, _, _ in mats.values())
+    bank_t = torch.from_numpy(synth.dense(max(maxK, maxM), 128, seed=5).ravel()).pin_memory()
+    if bf16:
+        bank_t = torch.from_numpy(synth.to_bf16_bits(bank_t.numpy())).pin_memory()
+    bank = bank_t.numpy()
+    arena_t = torch.empty(1 << 30, dtype=torch.float32).pin_memory()  # 4 GB of results
+    arena = arena_t.numpy()
+    keep, reqs, in_b, out_b, cursor = [], [], 0, 0, 0
+    for k in range(n_req):
+        A, n, _ = mats[ids[k]]
+        if is_spmm[k]:
+            B = bank[:A.K * n].reshape(A.K, n)
+            size = A.M * n
+        else:
+            B = bank[:A.M * n].reshape(A.M, n)
+            Y = bank[:A.K * n].reshape(A.K, n)
+            size = A.nnz
+        if cursor + size > arena.size:
+            cursor = 0
+        out = arena[cursor:cursor + size]
+        cursor += (size + 63) // 64 * 64
+        if is_spmm[k]:
+            reqs.append(Server.request(N_.OP_SPMM, ids[k], B, out.reshape(A.M, n)))
+            in_b += B.nbytes
+        else:
+            reqs.append(Server.request(N_.OP_SDDMM, ids[k], B, out, Y=Y))
+            in_b += B.nbytes + Y.nbytes
+        out_b += size * 4
+    result = {"workload": "%d requests, Poisson arrivals at 20k/s, SpMM or SDDMM 50/50, matrix "
+                          "ids from a 1024-matrix pool (%d distinct used; recent-id repeats "
+                          "p=0.8 over the last 8 ids), dense operands %s from pinned host memory"
+                          % (n_req, len(mats), "bf16" if bf16 else "fp32"),
+              "h2d_bytes": in_b, "d2h_bytes": out_b}
+    for mode, flags in (("batched", 0), ("per_call", N_.SERVER_PER_CALL)):
+        with Server(flags=flags, slots=1 if flags else 3) as srv:
+            for m, (A, _, _) in mats.items():
+                srv.add_matrix(m, A, pin=True)
+            srv.wait(srv.replay(reqs, arrivals)[-1], -1)  # cold pass: fills the cache
+            srv.drain(-1)
+            srv.stats(reset=True)
+            tickets = srv.replay(reqs, arrivals)
+            srv.drain(-1)
+            st = srv.stats()
+            bad = sum(1 for t in tickets if srv.wait(t, 0) != N_.OK)
+        result[mode] = {"requests_per_s": round(st["completed"] / st["span_s"], 1),
+                        "p50_us": round(st["p50_us"], 1), "p99_us": round(st["p99_us"], 1),
+                        "max_us": round(st["max_us"], 1), "mean_batch": round(st["mean_batch"], 2),
+                        "batches": st["batches"], "span_ms": round(st["span_s"] * 1e3, 2),
+                        "failed": bad}
+    result["throughput_vs_per_call"] = round(result["batched"]["requests_per_s"] /
+                                             result["per_call"]["requests_per_s"], 3)
+    result["p99_vs_per_call"] = round(result["per_call"]["p99_us"] /
+                                      max(result["batched"]["p99_us"], 1e-9), 3)
+    return result
+
+
 def run_ours(args, world, rank, local):
     import numpy as np
     import torch
@@ -429,6 +520,9 @@ def run_ours(args, world, rank, local):
     batched = None
     if not args.no_batched:
         batched = run_batched(args, N_, ops, stream)
+    served = None
+    if not args.no_serving:
+        served = run_serving(args, N_)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -456,7 +550,7 @@ def run_ours(args, world, rank, local):
                          "kernel_ms": round(kern_ms, 4), "peak_source": peak_kind + " hbm_gbs"},
             "gpu_launches": args.steps * (2 if eb else 1),
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks, "schedules": schedules,
-            "vendor": vendor, "batched": batched,
+            "vendor": vendor, "batched": batched, "served": served,
         }
         print(json.dumps(line), flush=True)
 
@@ -478,6 +572,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-vendor", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup(args)

@@ -158,11 +158,104 @@ int segtaco_batch_create(int32_t count, const segtaco_spmm_problem *problems,
 int segtaco_batch_run(segtaco_batch *batch, void *stream);
 /* Same, through a CUDA graph captured on the first call and replayed after. */
 int segtaco_batch_run_graph(segtaco_batch *batch, void *stream);
+/* Same as segtaco_batch_run, with problems released in order by a gate:
+ * problem i may run once *gate > i.  `gate` is device memory or mapped host
+ * memory that the caller raises while the launch runs.  Waits are bounded:
+ * after `timeout_ns` (at most 60 s) without release the kernels record
+ * SEGTACO_ETIMEOUT, read and cleared by segtaco_device_status(1), and end;
+ * products of problems never released are then not written. */
+int segtaco_batch_run_gated(segtaco_batch *batch, const int64_t *gate, int64_t timeout_ns,
+                            void *stream);
 /* Kernel-variant groups, total work items, and (if configs != NULL, count
  * entries) the configuration chosen for each problem. */
 int segtaco_batch_info(const segtaco_batch *batch, int32_t *groups, int64_t *items,
                        segtaco_config *configs);
 int segtaco_batch_destroy(segtaco_batch *batch);
+/* ---- Serving loop (segtaco_server_*) -------------------------------------
+ * A native scheduler thread admits SpMM and SDDMM requests as they arrive.
+ * CSR operands stay resident in a device cache keyed by matrix id (LRU, capped
+ * by bytes and by free HBM).  Whenever one of `slots` streams is idle, the
+ * pending requests that fit (staging bytes, cache room) form the next batch:
+ * their SpMMs run in one persistent batched launch, their SDDMMs beside it, and
+ * copies of one batch overlap the kernels of the others.  Failures complete a
+ * request with a status; nothing exits the process. */
+#define SEGTACO_OP_SPMM 0
+#define SEGTACO_OP_SDDMM 1
+
+#define SEGTACO_SERVER_PER_CALL 1u    /* one request per batch through the plain
+                                         segtaco_spmm path (per-call comparator)  */
+#define SEGTACO_SERVER_FAKE_DEVICE 2u /* tests of the host logic only: host memory
+                                         stands in for the device and no kernel
+                                         runs, so outputs are NOT written         */
+
+#define SEGTACO_REQ_DEVICE_DENSE 1u   /* dense operands and output are device
+                                         pointers (no staging copies)             */
+
+typedef struct segtaco_server_config {
+  int32_t max_batch;      /* requests per batch (0: 256)                          */
+  int32_t slots;          /* batches in flight, one stream each (0: 3)            */
+  int64_t cache_bytes;    /* device CSR cache cap (0: 120 GB), clamped to the
+                             free HBM at creation minus reserve_bytes             */
+  int64_t staging_bytes;  /* device bytes of staged dense operands in flight
+                             (0: 8 GB)                                            */
+  int64_t reserve_bytes;  /* HBM left free (0: 2 GB)                              */
+  uint32_t flags;         /* SEGTACO_SERVER_*                                     */
+  int32_t fail_alloc_at;  /* fault injection: the n-th device allocation
+                             (1-based) fails with ENOMEM; 0 = never               */
+  int32_t fake_delay_us;  /* FAKE_DEVICE: time a batch stays in flight            */
+  int32_t reserved;
+} segtaco_server_config;
+
+typedef struct segtaco_request {
+  int32_t op;       /* SEGTACO_OP_*                                               */
+  int32_t dtype;    /* dense operand type (SEGTACO_F32 / SEGTACO_BF16)            */
+  int64_t matrix;   /* id given to segtaco_server_add_matrix                      */
+  int32_t N;        /* SpMM: columns of B and C; SDDMM: D                         */
+  uint32_t flags;   /* SEGTACO_REQ_*                                              */
+  const void *B;    /* SpMM: B, K x N; SDDMM: X, M x D (row-major, dense)         */
+  const void *Y;    /* SDDMM: Y, K x D; unused for SpMM                           */
+  float *out;       /* SpMM: C, M x N; SDDMM: nnz values                          */
+} segtaco_request;
+
+typedef struct segtaco_server_stats {
+  int64_t submitted, completed, failed, cancelled, pending, in_flight;
+  int64_t batches, cache_hits, cache_misses, evictions, cache_bytes;
+  int64_t h2d_bytes, d2h_bytes;
+  double p50_us, p99_us, max_us, mean_us; /* arrival -> completion, requests
+                                             completed OK since the last reset   */
+  double span_s;                          /* first arrival -> last completion     */
+  double mean_batch;                      /* requests per batch                   */
+} segtaco_server_stats;
+
+typedef struct segtaco_server segtaco_server;
+int segtaco_server_create(const segtaco_server_config *cfg, segtaco_server **out);
+/* Registers host CSR arrays under `id` (checked here: row_ptr monotone from 0
+ * to nnz, 0 <= col < K).  The arrays must stay valid while the server lives;
+ * pinned host memory makes their uploads asynchronous.  vals NULL: all ones. */
+int segtaco_server_add_matrix(segtaco_server *srv, int64_t id, int32_t M, int32_t K,
+                              int64_t nnz, const int32_t *row_ptr, const int32_t *col,
+                              const float *vals);
+/* Queues a request; *ticket identifies it.  Requests naming an unknown matrix
+ * or an unsupported shape are refused here with SEGTACO_EINVAL. */
+int segtaco_server_submit(segtaco_server *srv, const segtaco_request *req, int64_t *ticket);
+/* Open-loop arrivals: submits reqs[i] at arrival_us[i] microseconds after the
+ * call starts (latency counts from that instant); returns once all are queued. */
+int segtaco_server_replay(segtaco_server *srv, int32_t n, const segtaco_request *reqs,
+                          const double *arrival_us, int64_t *tickets);
+/* Waits up to timeout_ms (< 0: forever) for a request: SEGTACO_OK with its
+ * final status in *status, or SEGTACO_ETIMEOUT if still running. */
+int segtaco_server_wait(segtaco_server *srv, int64_t ticket, int32_t timeout_ms,
+                        int32_t *status);
+/* Waits until nothing is pending or in flight. */
+int segtaco_server_drain(segtaco_server *srv, int32_t timeout_ms);
+/* Cancels a request not yet admitted (SEGTACO_OK; it completes with
+ * SEGTACO_ECANCELLED); SEGTACO_EBUSY once it is admitted or done. */
+int segtaco_server_cancel(segtaco_server *srv, int64_t ticket);
+int segtaco_server_get_stats(segtaco_server *srv, int32_t reset, segtaco_server_stats *out);
+/* Stops the scheduler: pending requests complete with SEGTACO_ECANCELLED,
+ * batches in flight finish first. */
+int segtaco_server_destroy(segtaco_server *srv);
+
 /* Row-length statistics of a device CSR (the autotuner's input):
  * stats[0] max row length, [1] empty rows, [2] rows >= 32, [3] nonzeros in
  * rows >= 32.  Synchronises `stream`. */

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <tuple>
 #include <vector>
 
@@ -85,67 +86,14 @@ __global__ void batch_partition_kernel(const BatchPartition *__restrict__ parts,
   }
 }
 
-}  // namespace segtaco
-
-using namespace segtaco;
-
-struct segtaco_batch {
-  struct Group {
-    int dtype, V, G;
-    bool rows;
-    std::vector<int> members;
-    long long total_items = 0;
-    size_t off_probs = 0, off_begin = 0;  // offsets into the device buffer
-    int grid = 0;
-  };
-  std::vector<segtaco_spmm_problem> problems;
-  std::vector<SpmmPlan> plans;
-  std::vector<segtaco_config> configs;
-  std::vector<Group> groups;
-  char *dmem = nullptr;
-  size_t dbytes = 0;
-  size_t off_parts = 0, off_queues = 0;
-  int nparts = 0;
-  long long total_edges = 0;
-  cudaGraphExec_t graph = nullptr;
-  int device = -1;
-};
-
+// ---------------------------------------------------------------------------
+// Descriptor layout, image and enqueue.
+// ---------------------------------------------------------------------------
 namespace {
-
-int enqueue(segtaco_batch *b, cudaStream_t s) {
-  if (!b->groups.empty())
-    SEGTACO_TRY(check_cuda(cudaMemsetAsync(b->dmem + b->off_queues, 0,
-                                           b->groups.size() * sizeof(unsigned long long), s),
-                           "memset queues"));
-  if (b->total_edges > 0) {
-    const long long blocks = (b->total_edges + 255) / 256;
-    batch_partition_kernel<<<(unsigned)blocks, 256, 0, s>>>(
-        reinterpret_cast<const BatchPartition *>(b->dmem + b->off_parts), b->nparts,
-        b->total_edges);
-    SEGTACO_TRY(check_launch("batch_partition_kernel"));
-  }
-  for (size_t gi = 0; gi < b->groups.size(); ++gi) {
-    const auto &g = b->groups[gi];
-    if (g.total_items == 0) continue;
-    BatchGroupLaunch L;
-    L.V = g.V;
-    L.G = g.G;
-    L.rows = g.rows;
-    L.probs = b->dmem + g.off_probs;
-    L.item_begin = reinterpret_cast<const long long *>(b->dmem + g.off_begin);
-    L.nprobs = (int)g.members.size();
-    L.total_items = g.total_items;
-    L.queue = reinterpret_cast<unsigned long long *>(b->dmem + b->off_queues) + gi;
-    L.grid = g.grid;
-    SEGTACO_TRY(g.dtype == SEGTACO_BF16 ? launch_batch_bf16(L, s) : launch_batch_f32(L, s));
-  }
-  return SEGTACO_OK;
-}
 
 template <typename BT>
 void fill_problem(BatchProblem<BT> &bp, const segtaco_spmm_problem &p, const SpmmPlan &plan,
-                  int *px, int *py, long long item_begin) {
+                  int *px, int *py, long long item_begin, int index) {
   memset(&bp, 0, sizeof(bp));
   SpmmArgs<BT> &a = bp.a;
   a.M = p.M;
@@ -166,9 +114,227 @@ void fill_problem(BatchProblem<BT> &bp, const segtaco_spmm_problem &p, const Spm
   a.l2_hints = plan.l2_hints ? 1 : 0;
   bp.item_begin = item_begin;
   bp.slabs = plan.slabs;
+  bp.index = index;
+}
+
+// Resident CTAs per SM of each batch kernel variant, per device (queried once).
+int blocks_per_sm(int device, int dtype, int V, int G, bool rows, int *out) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int, int, bool>, int> cache;
+  const auto key = std::make_tuple(device, dtype, V, G, rows);
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      *out = it->second;
+      return SEGTACO_OK;
+    }
+  }
+  int n = 0;
+  SEGTACO_TRY(dtype == SEGTACO_BF16 ? batch_blocks_per_sm_bf16(V, G, rows, &n)
+                                    : batch_blocks_per_sm_f32(V, G, rows, &n));
+  std::lock_guard<std::mutex> lk(mu);
+  cache[key] = n;
+  *out = n;
+  return SEGTACO_OK;
+}
+
+int sm_count(int device) {
+  static std::mutex mu;
+  static std::map<int, int> cache;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find(device);
+  if (it != cache.end()) return it->second;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) sms = 1;
+  cache[device] = sms;
+  return sms;
 }
 
 }  // namespace
+
+void batch_layout(const segtaco_spmm_problem *probs, const SpmmPlan *plans, int count,
+                  BatchLayout *L) {
+  *L = BatchLayout();
+  std::map<std::tuple<int, int, int, bool>, int> gidx;
+  for (int i = 0; i < count; ++i) {
+    const auto &p = probs[i];
+    if (p.M == 0 || p.N == 0) continue;
+    const auto &pl = plans[i];
+    const bool rows = pl.schedule == SEGTACO_RB_SR || pl.schedule == SEGTACO_RB_PR;
+    const auto key = std::make_tuple(p.b_dtype, pl.V, pl.G, rows);
+    auto it = gidx.find(key);
+    if (it == gidx.end()) {
+      it = gidx.emplace(key, (int)L->groups.size()).first;
+      BatchLayout::Group g;
+      g.dtype = p.b_dtype;
+      g.V = pl.V;
+      g.G = pl.G;
+      g.rows = rows;
+      L->groups.push_back(g);
+    }
+    L->groups[it->second].members.push_back(i);
+  }
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off += align256(bytes);
+    return o;
+  };
+  L->off_px.assign(count, 0);
+  L->off_py.assign(count, 0);
+  L->has_part.assign(count, 0);
+  for (int i = 0; i < count; ++i) {
+    const auto &pl = plans[i];
+    const bool eb = pl.schedule == SEGTACO_EB_SR || pl.schedule == SEGTACO_EB_PR;
+    if (eb && probs[i].M > 0 && probs[i].N > 0) {
+      L->has_part[i] = 1;
+      L->off_px[i] = take((pl.nchunks + 1) * sizeof(int));
+      L->off_py[i] = take((pl.nchunks + 1) * sizeof(int));
+      ++L->nparts;
+    }
+  }
+  L->off_parts = take(std::max(1, L->nparts) * sizeof(BatchPartition));
+  for (auto &g : L->groups) {
+    g.off_probs = take(g.members.size() * sizeof(BatchProblem<float>));
+    g.off_begin = take(g.members.size() * sizeof(long long));
+  }
+  L->off_queues = take(std::max<size_t>(1, L->groups.size()) * sizeof(unsigned long long));
+  L->bytes = off;
+}
+
+int batch_image(const segtaco_spmm_problem *probs, const SpmmPlan *plans, int count,
+                BatchLayout *L, char *dbase, char *img, int device) {
+  std::vector<BatchPartition> parts;
+  long long edges = 0;
+  for (int i = 0; i < count; ++i) {
+    if (!L->has_part[i]) continue;
+    const auto &p = probs[i];
+    const auto &pl = plans[i];
+    BatchPartition bp;
+    bp.row_ptr = p.row_ptr;
+    bp.M = p.M;
+    bp.nnz = p.nnz;
+    bp.D = pl.items_per_unit;
+    bp.nchunks = pl.nchunks;
+    bp.px = reinterpret_cast<int *>(dbase + L->off_px[i]);
+    bp.py = reinterpret_cast<int *>(dbase + L->off_py[i]);
+    bp.C = p.C;
+    bp.ldc = p.ldc;
+    bp.N = p.N;
+    bp.edge_begin = edges;
+    edges += pl.nchunks + 1;
+    parts.push_back(bp);
+  }
+  L->total_edges = edges;
+  if (!parts.empty())
+    memcpy(img + L->off_parts, parts.data(), parts.size() * sizeof(BatchPartition));
+  const int sms = sm_count(device);
+  for (auto &g : L->groups) {
+    long long item = 0;
+    std::vector<long long> begin;
+    begin.reserve(g.members.size());
+    for (size_t k = 0; k < g.members.size(); ++k) {
+      const int i = g.members[k];
+      const auto &pl = plans[i];
+      int *px = L->has_part[i] ? reinterpret_cast<int *>(dbase + L->off_px[i]) : nullptr;
+      int *py = L->has_part[i] ? reinterpret_cast<int *>(dbase + L->off_py[i]) : nullptr;
+      begin.push_back(item);
+      if (g.dtype == SEGTACO_BF16) {
+        BatchProblem<uint16_t> bp;
+        fill_problem(bp, probs[i], pl, px, py, item, i);
+        memcpy(img + g.off_probs + k * sizeof(bp), &bp, sizeof(bp));
+      } else {
+        BatchProblem<float> bp;
+        fill_problem(bp, probs[i], pl, px, py, item, i);
+        memcpy(img + g.off_probs + k * sizeof(bp), &bp, sizeof(bp));
+      }
+      item += pl.nchunks * (long long)pl.slabs;
+    }
+    g.total_items = item;
+    memcpy(img + g.off_begin, begin.data(), begin.size() * sizeof(long long));
+    // Persistent grid: every SM full, never more CTAs than the items need.
+    int per_sm = 0;
+    SEGTACO_TRY(blocks_per_sm(device, g.dtype, g.V, g.G, g.rows, &per_sm));
+    const long long need = (item + (kCta / 32) - 1) / (kCta / 32);
+    long long grid = (long long)std::max(1, per_sm) * std::max(1, sms);
+    if (grid > need) grid = std::max(1LL, need);
+    g.grid = (int)grid;
+  }
+  return SEGTACO_OK;
+}
+
+int batch_enqueue(const BatchLayout &L, char *dbase, cudaStream_t s, const BatchGate *gate) {
+  if (!L.groups.empty())
+    SEGTACO_TRY(check_cuda(cudaMemsetAsync(dbase + L.off_queues, 0,
+                                           L.groups.size() * sizeof(unsigned long long), s),
+                           "memset queues"));
+  if (L.total_edges > 0) {
+    const long long blocks = (L.total_edges + 255) / 256;
+    batch_partition_kernel<<<(unsigned)blocks, 256, 0, s>>>(
+        reinterpret_cast<const BatchPartition *>(dbase + L.off_parts), L.nparts, L.total_edges);
+    SEGTACO_TRY(check_launch("batch_partition_kernel"));
+  }
+  for (size_t gi = 0; gi < L.groups.size(); ++gi) {
+    const auto &g = L.groups[gi];
+    if (g.total_items == 0) continue;
+    BatchGroupLaunch G;
+    G.V = g.V;
+    G.G = g.G;
+    G.rows = g.rows;
+    G.probs = dbase + g.off_probs;
+    G.item_begin = reinterpret_cast<const long long *>(dbase + g.off_begin);
+    G.nprobs = (int)g.members.size();
+    G.total_items = g.total_items;
+    G.queue = reinterpret_cast<unsigned long long *>(dbase + L.off_queues) + gi;
+    G.grid = g.grid;
+    G.gate = gate ? *gate : BatchGate{nullptr, 0, nullptr};
+    SEGTACO_TRY(g.dtype == SEGTACO_BF16 ? launch_batch_bf16(G, s) : launch_batch_f32(G, s));
+  }
+  return SEGTACO_OK;
+}
+
+// Validates a problem and resolves its plan: the caller's config, or the
+// heuristic on `max_row_len`.  Ring and partition-ready flags are cleared and
+// the depth reset (batch kernels keep four loads in flight).
+int check_batch_problem(const segtaco_spmm_problem &p, int index) {
+  if (p.M < 0 || p.K < 0 || p.N < 0 || p.nnz < 0 || p.nnz > 0x7fffffffLL ||
+      (p.M > 0 && !p.row_ptr) || (p.nnz > 0 && (!p.col || !p.B)) ||
+      (p.M > 0 && p.N > 0 && !p.C) || p.ldb < p.N || p.ldc < p.N ||
+      (p.b_dtype != SEGTACO_F32 && p.b_dtype != SEGTACO_BF16))
+    return set_error(SEGTACO_EINVAL, "batch: problem %d is malformed", index);
+  return SEGTACO_OK;
+}
+
+int plan_batch_problem(const segtaco_spmm_problem &p, const segtaco_config *cfg,
+                       long long max_row_len, int index, segtaco_config *used, SpmmPlan *plan) {
+  SEGTACO_TRY(check_batch_problem(p, index));
+  segtaco_config c;
+  if (cfg) {
+    c = *cfg;
+  } else {
+    c.schedule = SEGTACO_AUTO;
+    segtaco_autotune_heuristic(p.M, p.K, p.nnz, p.N, p.b_dtype, max_row_len, &c);
+  }
+  c.depth = 0;
+  c.flags &= ~(SEGTACO_FLAG_SMEM_RING | SEGTACO_FLAG_TMA_BULK | SEGTACO_FLAG_PARTITION_READY);
+  *used = c;
+  return plan_spmm(p.M, p.K, p.nnz, p.N, p.b_dtype, p.ldb, p.ldc, p.B, p.C, &c, plan);
+}
+
+}  // namespace segtaco
+
+using namespace segtaco;
+
+struct segtaco_batch {
+  std::vector<segtaco_spmm_problem> problems;
+  std::vector<SpmmPlan> plans;
+  std::vector<segtaco_config> configs;
+  BatchLayout layout;
+  char *dmem = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int device = -1;
+};
 
 extern "C" {
 
@@ -198,153 +364,39 @@ int segtaco_batch_create(int32_t count, const segtaco_spmm_problem *problems,
     segtaco_batch_destroy(b);
     return st;
   };
-  cudaGetDevice(&b->device);
   b->problems.assign(problems, problems + count);
   b->configs.resize(count);
   b->plans.resize(count);
-  // ---- configs: the caller's, or the heuristic on device row statistics ----
-  std::vector<int64_t> stats(4 * (size_t)count, 0);
-  if (!configs) {
-    for (int i = 0; i < count; ++i) {
-      const auto &p = b->problems[i];
-      if (p.M > 0) {
-        const int st = segtaco_row_stats(p.M, p.row_ptr, &stats[4 * (size_t)i], stream);
-        if (st != SEGTACO_OK) return fail(st);
-      }
-    }
-  }
+  // Validate every problem before any device work.
   for (int i = 0; i < count; ++i) {
-    const auto &p = b->problems[i];
-    if (p.M < 0 || p.K < 0 || p.N < 0 || p.nnz < 0 || p.nnz > 0x7fffffffLL ||
-        (p.M > 0 && !p.row_ptr) ||
-        (p.nnz > 0 && (!p.col || !p.B)) || (p.M > 0 && p.N > 0 && !p.C) || p.ldb < p.N ||
-        p.ldc < p.N || (p.b_dtype != SEGTACO_F32 && p.b_dtype != SEGTACO_BF16))
-      return fail(set_error(SEGTACO_EINVAL, "segtaco_batch_create: problem %d is malformed", i));
-    segtaco_config c;
-    if (configs) {
-      c = configs[i];
-    } else {
-      c.schedule = SEGTACO_AUTO;
-      segtaco_autotune_heuristic(p.M, p.K, p.nnz, p.N, p.b_dtype, stats[4 * (size_t)i], &c);
-    }
-    c.depth = 0;                          // batch kernels keep 4 loads in flight
-    c.flags &= ~(SEGTACO_FLAG_SMEM_RING | SEGTACO_FLAG_TMA_BULK | SEGTACO_FLAG_PARTITION_READY);
-    b->configs[i] = c;
-    const int st = plan_spmm(p.M, p.K, p.nnz, p.N, p.b_dtype, p.ldb, p.ldc, p.B, p.C, &c,
-                             &b->plans[i]);
+    const int st = check_batch_problem(b->problems[i], i);
     if (st != SEGTACO_OK) return fail(st);
   }
-  // ---- groups by kernel variant ----
-  std::map<std::tuple<int, int, int, bool>, int> gidx;
+  cudaGetDevice(&b->device);
   for (int i = 0; i < count; ++i) {
     const auto &p = b->problems[i];
-    if (p.M == 0 || p.N == 0) continue;
-    const auto &pl = b->plans[i];
-    const bool rows = pl.schedule == SEGTACO_RB_SR || pl.schedule == SEGTACO_RB_PR;
-    const auto key = std::make_tuple(p.b_dtype, pl.V, pl.G, rows);
-    auto it = gidx.find(key);
-    if (it == gidx.end()) {
-      it = gidx.emplace(key, (int)b->groups.size()).first;
-      segtaco_batch::Group g;
-      g.dtype = p.b_dtype;
-      g.V = pl.V;
-      g.G = pl.G;
-      g.rows = rows;
-      b->groups.push_back(g);
+    int64_t stats[4] = {0, 0, 0, 0};
+    if (!configs && p.M > 0) {
+      const int st = segtaco_row_stats(p.M, p.row_ptr, stats, stream);
+      if (st != SEGTACO_OK) return fail(st);
     }
-    b->groups[it->second].members.push_back(i);
+    const int st = plan_batch_problem(p, configs ? &configs[i] : nullptr, stats[0], i,
+                                      &b->configs[i], &b->plans[i]);
+    if (st != SEGTACO_OK) return fail(st);
   }
-  // ---- device buffer layout ----
-  size_t off = 0;
-  auto take = [&](size_t bytes) {
-    const size_t o = off;
-    off += align256(bytes);
-    return o;
-  };
-  std::vector<size_t> off_px(count, 0), off_py(count, 0);
-  std::vector<char> has_part(count, 0);
-  for (int i = 0; i < count; ++i) {
-    const auto &pl = b->plans[i];
-    const bool eb = pl.schedule == SEGTACO_EB_SR || pl.schedule == SEGTACO_EB_PR;
-    if (eb && b->problems[i].M > 0 && b->problems[i].N > 0) {
-      has_part[i] = 1;
-      off_px[i] = take((pl.nchunks + 1) * sizeof(int));
-      off_py[i] = take((pl.nchunks + 1) * sizeof(int));
-      ++b->nparts;
-    }
-  }
-  b->off_parts = take(std::max(1, b->nparts) * sizeof(BatchPartition));
-  for (auto &g : b->groups) {
-    g.off_probs = take(g.members.size() * sizeof(BatchProblem<float>));
-    g.off_begin = take(g.members.size() * sizeof(long long));
-  }
-  b->off_queues = take(std::max<size_t>(1, b->groups.size()) * sizeof(unsigned long long));
-  b->dbytes = off;
+  batch_layout(b->problems.data(), b->plans.data(), count, &b->layout);
   {
-    cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&b->dmem), b->dbytes);
+    cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&b->dmem), b->layout.bytes);
     if (e != cudaSuccess) return fail(check_cuda(e, "cudaMalloc(batch)"));
   }
-  // ---- host images of the descriptors ----
-  std::vector<char> himg(b->dbytes, 0);
-  std::vector<BatchPartition> parts;
-  long long edges = 0;
-  for (int i = 0; i < count; ++i) {
-    if (!has_part[i]) continue;
-    const auto &p = b->problems[i];
-    const auto &pl = b->plans[i];
-    BatchPartition bp;
-    bp.row_ptr = p.row_ptr;
-    bp.M = p.M;
-    bp.nnz = p.nnz;
-    bp.D = pl.items_per_unit;
-    bp.nchunks = pl.nchunks;
-    bp.px = reinterpret_cast<int *>(b->dmem + off_px[i]);
-    bp.py = reinterpret_cast<int *>(b->dmem + off_py[i]);
-    bp.C = p.C;
-    bp.ldc = p.ldc;
-    bp.N = p.N;
-    bp.edge_begin = edges;
-    edges += pl.nchunks + 1;
-    parts.push_back(bp);
-  }
-  b->total_edges = edges;
-  if (!parts.empty())
-    memcpy(himg.data() + b->off_parts, parts.data(), parts.size() * sizeof(BatchPartition));
-  for (auto &g : b->groups) {
-    long long item = 0;
-    std::vector<long long> begin;
-    for (size_t k = 0; k < g.members.size(); ++k) {
-      const int i = g.members[k];
-      const auto &pl = b->plans[i];
-      int *px = has_part[i] ? reinterpret_cast<int *>(b->dmem + off_px[i]) : nullptr;
-      int *py = has_part[i] ? reinterpret_cast<int *>(b->dmem + off_py[i]) : nullptr;
-      begin.push_back(item);
-      if (g.dtype == SEGTACO_BF16) {
-        BatchProblem<uint16_t> bp;
-        fill_problem(bp, b->problems[i], pl, px, py, item);
-        memcpy(himg.data() + g.off_probs + k * sizeof(bp), &bp, sizeof(bp));
-      } else {
-        BatchProblem<float> bp;
-        fill_problem(bp, b->problems[i], pl, px, py, item);
-        memcpy(himg.data() + g.off_probs + k * sizeof(bp), &bp, sizeof(bp));
-      }
-      item += pl.nchunks * (long long)pl.slabs;
-    }
-    g.total_items = item;
-    memcpy(himg.data() + g.off_begin, begin.data(), begin.size() * sizeof(long long));
-    // Persistent grid: every SM full, never more CTAs than items need.
-    int per_sm = 0, sms = 0;
-    const int st = g.dtype == SEGTACO_BF16 ? batch_blocks_per_sm_bf16(g.V, g.G, g.rows, &per_sm)
-                                           : batch_blocks_per_sm_f32(g.V, g.G, g.rows, &per_sm);
+  std::vector<char> himg(b->layout.bytes, 0);
+  {
+    const int st = batch_image(b->problems.data(), b->plans.data(), count, &b->layout, b->dmem,
+                               himg.data(), b->device);
     if (st != SEGTACO_OK) return fail(st);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
-    const long long need = (item + (kCta / 32) - 1) / (kCta / 32);
-    long long grid = (long long)std::max(1, per_sm) * std::max(1, sms);
-    if (grid > need) grid = std::max(1LL, need);
-    g.grid = (int)grid;
   }
   {
-    const int st = check_cuda(cudaMemcpyAsync(b->dmem, himg.data(), b->dbytes,
+    const int st = check_cuda(cudaMemcpyAsync(b->dmem, himg.data(), b->layout.bytes,
                                               cudaMemcpyHostToDevice, s),
                               "upload batch descriptors");
     if (st != SEGTACO_OK) return fail(st);
@@ -357,7 +409,7 @@ int segtaco_batch_create(int32_t count, const segtaco_spmm_problem *problems,
 
 int segtaco_batch_run(segtaco_batch *b, void *stream) {
   if (!b) return set_error(SEGTACO_EINVAL, "batch is NULL");
-  return enqueue(b, static_cast<cudaStream_t>(stream));
+  return batch_enqueue(b->layout, b->dmem, static_cast<cudaStream_t>(stream));
 }
 
 int segtaco_batch_run_graph(segtaco_batch *b, void *stream) {
@@ -370,7 +422,7 @@ int segtaco_batch_run_graph(segtaco_batch *b, void *stream) {
     cudaGraph_t graph = nullptr;
     int st = check_cuda(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "capture");
     if (st == SEGTACO_OK) {
-      const int est = enqueue(b, cs);
+      const int est = batch_enqueue(b->layout, b->dmem, cs);
       const int cst = check_cuda(cudaStreamEndCapture(cs, &graph), "end capture");
       st = est != SEGTACO_OK ? est : cst;
     }
@@ -383,13 +435,25 @@ int segtaco_batch_run_graph(segtaco_batch *b, void *stream) {
   return check_cuda(cudaGraphLaunch(b->graph, s), "cudaGraphLaunch");
 }
 
+int segtaco_batch_run_gated(segtaco_batch *b, const int64_t *gate, int64_t timeout_ns,
+                            void *stream) {
+  if (!b || !gate) return set_error(SEGTACO_EINVAL, "batch or gate is NULL");
+  if (timeout_ns <= 0 || timeout_ns > 60LL * 1000000000LL)
+    return set_error(SEGTACO_EINVAL, "gate timeout must be in (0, 60 s]");
+  BatchGate g;
+  g.gate = reinterpret_cast<const volatile long long *>(gate);
+  g.timeout_ns = timeout_ns;
+  SEGTACO_TRY(tma_status_ptr(&g.status));
+  return batch_enqueue(b->layout, b->dmem, static_cast<cudaStream_t>(stream), &g);
+}
+
 int segtaco_batch_info(const segtaco_batch *b, int32_t *groups, int64_t *items,
                        segtaco_config *configs) {
   if (!b) return set_error(SEGTACO_EINVAL, "batch is NULL");
-  if (groups) *groups = (int32_t)b->groups.size();
+  if (groups) *groups = (int32_t)b->layout.groups.size();
   if (items) {
     long long t = 0;
-    for (const auto &g : b->groups) t += g.total_items;
+    for (const auto &g : b->layout.groups) t += g.total_items;
     *items = t;
   }
   if (configs)

@@ -9,7 +9,7 @@ namespace segtaco {
   case V * 100 + G:                                                                        \
     spmm_batch_kernel<uint16_t, V, G, R><<<g.grid, kCta, 0, s>>>(                            \
         static_cast<const BatchProblem<uint16_t> *>(g.probs), g.item_begin, g.nprobs,         \
-        g.total_items, g.queue);                                                           \
+        g.total_items, g.queue, g.gate);                                                           \
     break;
 #define SEGTACO_BATCH_OCC(V, G, R)                                                         \
   case V * 100 + G:                                                                        \

@@ -68,6 +68,38 @@ class SpmmProblem(C.Structure):
                 ("ldc", C.c_int64)]
 
 
+OP_SPMM, OP_SDDMM = 0, 1
+SERVER_PER_CALL, SERVER_FAKE_DEVICE = 1, 2
+REQ_DEVICE_DENSE = 1
+
+
+class ServerConfig(C.Structure):
+    """segtaco_server_config: zero fields take the defaults."""
+    _fields_ = [("max_batch", C.c_int32), ("slots", C.c_int32), ("cache_bytes", C.c_int64),
+                ("staging_bytes", C.c_int64), ("reserve_bytes", C.c_int64),
+                ("flags", C.c_uint32), ("fail_alloc_at", C.c_int32),
+                ("fake_delay_us", C.c_int32), ("reserved", C.c_int32)]
+
+
+class Request(C.Structure):
+    """segtaco_request."""
+    _fields_ = [("op", C.c_int32), ("dtype", C.c_int32), ("matrix", C.c_int64),
+                ("N", C.c_int32), ("flags", C.c_uint32), ("B", C.c_void_p), ("Y", C.c_void_p),
+                ("out", C.c_void_p)]
+
+
+class ServerStats(C.Structure):
+    """segtaco_server_stats."""
+    _fields_ = [(f, C.c_int64) for f in (
+        "submitted", "completed", "failed", "cancelled", "pending", "in_flight", "batches",
+        "cache_hits", "cache_misses", "evictions", "cache_bytes", "h2d_bytes", "d2h_bytes")] + \
+        [(f, C.c_double) for f in ("p50_us", "p99_us", "max_us", "mean_us", "span_s",
+                                   "mean_batch")]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 class TacoTensor(C.Structure):
     """taco_tensor_t (segTACO taco_tensor_t.h:6-15), same layout."""
     _fields_ = [("order", C.c_int32), ("dimensions", C.POINTER(C.c_int32)),
@@ -97,9 +129,20 @@ SIGNATURES = {
                                        C.POINTER(_P)]),
     "segtaco_batch_run": (C.c_int, [_P, _P]),
     "segtaco_batch_run_graph": (C.c_int, [_P, _P]),
+    "segtaco_batch_run_gated": (C.c_int, [_P, _P, _I64, _P]),
     "segtaco_batch_info": (C.c_int, [_P, C.POINTER(_I), C.POINTER(_I64), C.POINTER(Config)]),
     "segtaco_batch_destroy": (C.c_int, [_P]),
     "segtaco_row_stats": (C.c_int, [_I, _P, C.POINTER(_I64), _P]),
+    "segtaco_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(_P)]),
+    "segtaco_server_add_matrix": (C.c_int, [_P, _I64, _I, _I, _I64, _P, _P, _P]),
+    "segtaco_server_submit": (C.c_int, [_P, C.POINTER(Request), C.POINTER(_I64)]),
+    "segtaco_server_replay": (C.c_int, [_P, _I, C.POINTER(Request), C.POINTER(C.c_double),
+                                        C.POINTER(_I64)]),
+    "segtaco_server_wait": (C.c_int, [_P, _I64, _I, C.POINTER(_I)]),
+    "segtaco_server_drain": (C.c_int, [_P, _I]),
+    "segtaco_server_cancel": (C.c_int, [_P, _I64]),
+    "segtaco_server_get_stats": (C.c_int, [_P, _I, C.POINTER(ServerStats)]),
+    "segtaco_server_destroy": (C.c_int, [_P]),
     "segtaco_block_starts_taco": (C.c_int, [_I, _I64, _P, _I, _P, _P]),
     "segtaco_block_starts_canonical": (C.c_int, [_I, _I64, _P, _I, _P, _P]),
     "segtaco_merge_path": (C.c_int, [_I, _I64, _P, _I64, _P, _P, _P]),

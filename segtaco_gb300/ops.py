@@ -215,6 +215,12 @@ class Batch:
         fn = N.lib().segtaco_batch_run_graph if graph else N.lib().segtaco_batch_run
         N.check(fn(self._h, _stream(stream)))
 
+    def run_gated(self, gate: torch.Tensor, timeout_s: float = 1.0, stream=None):
+        """Run with problems released by `gate` (int64 device tensor, or pinned
+        host tensor): problem i runs once gate[0] > i."""
+        N.check(N.lib().segtaco_batch_run_gated(self._h, C.c_void_p(gate.data_ptr()),
+                                                int(timeout_s * 1e9), _stream(stream)))
+
     def info(self):
         g = C.c_int32()
         it = C.c_int64()
