@@ -309,6 +309,33 @@ def run_batched(args, N_, ops, stream, count=256):
     }
 
 
+def run_gather_ceiling(ops, stream, reps=5):
+    """Random-row gather throughput of this GPU (segtaco_probe_gather) over
+    buffers that fit in L2 and buffers that do not: the ceilings that bound
+    SpMM with scattered columns (each nonzero gathers one dense row slice)."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    big = torch.empty(1 << 30, dtype=torch.uint8, device="cuda")
+    out = {}
+    for mb in (32, 64, 96, 128, 256, 1024):
+        buf = big[:mb << 20]
+        for rb in (64, 128, 512):
+            n = (6 << 30) // rb
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            for _ in range(2):
+                ops.probe_gather(buf, rb, n, sms * 8, stream=stream)
+            ev[0].record(stream)
+            for i in range(reps):
+                ops.probe_gather(buf, rb, n, sms * 8, seed=i, stream=stream)
+            ev[1].record(stream)
+            torch.cuda.synchronize()
+            sec = ev[0].elapsed_time(ev[1]) / reps / 1e3
+            out["%dMB_%dB" % (mb, rb)] = {"GBps": round(n * rb / sec / 1e9, 1),
+                                          "Glines_per_s": round(n * max(rb, 128) / 128 / sec / 1e9, 2)}
+    del big
+    return out
+
+
 def serving_stream(n_req, pool_size=1024, lam=20000.0, recent=8, p_repeat=0.8, seed=0):
     """Request stream of the serving workload: Poisson arrivals at `lam` per
     second, op SpMM or SDDMM 50/50, matrix id one of the `recent` most recently
@@ -523,6 +550,9 @@ def run_ours(args, world, rank, local):
     served = None
     if not args.no_serving:
         served = run_serving(args, N_)
+    ceiling = None
+    if not args.no_probe:
+        ceiling = run_gather_ceiling(ops, stream)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -551,6 +581,7 @@ def run_ours(args, world, rank, local):
             "gpu_launches": args.steps * (2 if eb else 1),
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks, "schedules": schedules,
             "vendor": vendor, "batched": batched, "served": served,
+            "gather_ceiling": ceiling,
         }
         print(json.dumps(line), flush=True)
 
@@ -573,6 +604,7 @@ def main():
     ap.add_argument("--no-vendor", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-probe", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup(args)

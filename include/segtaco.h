@@ -256,6 +256,13 @@ int segtaco_server_get_stats(segtaco_server *srv, int32_t reset, segtaco_server_
  * batches in flight finish first. */
 int segtaco_server_destroy(segtaco_server *srv);
 
+/* Diagnostic: n gathers of row_bytes-byte rows (16..512, a power of two) at
+ * pseudo-random rows of buf (rows x row_bytes bytes, 16-byte aligned) by a
+ * persistent grid of `blocks` CTAs of 256 threads.  Timing it gives the
+ * random-gather ceiling that bounds SpMM with scattered columns. */
+int segtaco_probe_gather(const void *buf, int64_t rows, int32_t row_bytes, int64_t n,
+                         uint32_t seed, float *sink, int32_t blocks, void *stream);
+
 /* Row-length statistics of a device CSR (the autotuner's input):
  * stats[0] max row length, [1] empty rows, [2] rows >= 32, [3] nonzeros in
  * rows >= 32.  Synchronises `stream`. */

@@ -177,6 +177,18 @@ def csr_validate(A: DeviceCSR, stream=None):
                                          _stream(stream)))
 
 
+def probe_gather(buf: torch.Tensor, row_bytes: int, n: int, blocks: int, seed: int = 0,
+                 sink: torch.Tensor | None = None, stream=None):
+    """Enqueue n random row gathers of row_bytes over device buffer `buf`."""
+    nbytes = buf.numel() * buf.element_size()
+    if sink is None:
+        sink = torch.zeros(32, dtype=torch.float32, device=buf.device)
+    N.check(N.lib().segtaco_probe_gather(C.c_void_p(buf.data_ptr()), nbytes // row_bytes,
+                                         row_bytes, n, seed, C.c_void_p(sink.data_ptr()), blocks,
+                                         _stream(stream)))
+    return sink
+
+
 def row_stats(A: DeviceCSR, stream=None):
     """Row-length statistics: (max length, empty rows, rows >= 32, nonzeros in rows >= 32)."""
     out = (C.c_int64 * 4)()
