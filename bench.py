@@ -314,7 +314,6 @@ def run_gather_ceiling(ops, stream, reps=5):
     buffers that fit in L2 and buffers that do not: the ceilings that bound
     SpMM with scattered columns (each nonzero gathers one dense row slice)."""
     import torch
-    sms = torch.cuda.get_device_properties(0).multi_processor_count
     big = torch.empty(1 << 30, dtype=torch.uint8, device="cuda")
     out = {}
     for mb in (32, 64, 96, 128, 256, 1024):
@@ -323,10 +322,10 @@ def run_gather_ceiling(ops, stream, reps=5):
             n = (6 << 30) // rb
             ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
             for _ in range(2):
-                ops.probe_gather(buf, rb, n, sms * 8, stream=stream)
+                ops.probe_gather(buf, rb, n, 0, stream=stream)
             ev[0].record(stream)
             for i in range(reps):
-                ops.probe_gather(buf, rb, n, sms * 8, seed=i, stream=stream)
+                ops.probe_gather(buf, rb, n, 0, seed=i, stream=stream)
             ev[1].record(stream)
             torch.cuda.synchronize()
             sec = ev[0].elapsed_time(ev[1]) / reps / 1e3
@@ -457,6 +456,10 @@ def run_ours(args, world, rank, local):
         cfg.items_per_unit = args.items
     if args.l2_hints:
         cfg.flags |= N_.FLAG_L2_HINTS
+    if args.row_walk:
+        cfg.flags |= N_.FLAG_ROW_WALK
+    if args.flat_walk:
+        cfg.flags |= N_.FLAG_FLAT_WALK
     ws_bytes = max(256, ops.spmm_workspace_size(Ad, N, N_.F32, cfg))
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
 
@@ -465,7 +468,7 @@ def run_ours(args, world, rank, local):
     if args.all_schedules:
         for s in ("rb_sr", "rb_pr", "eb_sr", "eb_pr"):
             c = tuned(N_.SCHEDULES[s])
-            c.flags |= cfg.flags & N_.FLAG_L2_HINTS
+            c.flags |= cfg.flags & (N_.FLAG_L2_HINTS | N_.FLAG_ROW_WALK | N_.FLAG_FLAT_WALK)
             wsz = max(256, ops.spmm_workspace_size(Ad, N, N_.F32, c))
             w = torch.empty(wsz, dtype=torch.uint8, device="cuda")
             st, kt = time_spmm(ops, N_, Ad, Bd, Cd, c, w, stream, max(3, args.steps // 2), 2)
@@ -577,6 +580,8 @@ def run_ours(args, world, rank, local):
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "traffic": traffic, "kernel": kernel_name,
+                         "gathered_bytes": A.nnz * N * 4,
+                         "gather_GBps": round(A.nnz * N * 4 / kern_ms / 1e6, 1),
                          "kernel_ms": round(kern_ms, 4), "peak_source": peak_kind + " hbm_gbs"},
             "gpu_launches": args.steps * (2 if eb else 1),
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks, "schedules": schedules,
@@ -597,6 +602,8 @@ def main():
     ap.add_argument("--col-tile", type=int, default=0)
     ap.add_argument("--items", type=int, default=0)
     ap.add_argument("--l2-hints", action="store_true")
+    ap.add_argument("--row-walk", action="store_true")
+    ap.add_argument("--flat-walk", action="store_true")
     ap.add_argument("--all-schedules", action="store_true", default=True)
     ap.add_argument("--no-all-schedules", dest="all_schedules", action="store_false")
     ap.add_argument("--no-e2e", action="store_true")

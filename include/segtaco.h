@@ -63,6 +63,11 @@ extern "C" {
                                      them into registers */
 #define SEGTACO_FLAG_TMA_BULK 8u  /* with SMEM_RING: fill the ring with cp.async.bulk
                                      (TMA) copies rather than 16-byte cp.async copies */
+#define SEGTACO_FLAG_ROW_WALK 16u /* walk each unit row by row (the default except
+                                     for eb_sr; depth 4 or 8 loads in flight)    */
+#define SEGTACO_FLAG_FLAT_WALK 32u /* walk each unit in batches of 32 nonzeros
+                                      across rows (the default for eb_sr with
+                                      16-byte vectors)                           */
 
 /* Tuning knobs.  Zero in a field means "choose automatically". */
 typedef struct segtaco_config {
@@ -72,7 +77,7 @@ typedef struct segtaco_config {
   int32_t rows_per_unit;  /* rb: rows handled by one lane group / warp            */
   int32_t items_per_unit; /* eb: merge-path items (rows + nonzeros) per unit      */
   uint32_t flags;         /* SEGTACO_FLAG_*                                        */
-  int32_t depth;          /* dense loads in flight per lane (0 = automatic, 4 or 8) */
+  int32_t depth;          /* row walk: dense loads in flight per lane (0 = 4, 4, 8) */
 } segtaco_config;
 
 /* Library identity and build checks. */
@@ -258,10 +263,16 @@ int segtaco_server_destroy(segtaco_server *srv);
 
 /* Diagnostic: n gathers of row_bytes-byte rows (16..512, a power of two) at
  * pseudo-random rows of buf (rows x row_bytes bytes, 16-byte aligned) by a
- * persistent grid of `blocks` CTAs of 256 threads.  Timing it gives the
+ * persistent grid of `blocks` CTAs of 256 threads (0: one full resident wave).  Timing it gives the
  * random-gather ceiling that bounds SpMM with scattered columns. */
 int segtaco_probe_gather(const void *buf, int64_t rows, int32_t row_bytes, int64_t n,
                          uint32_t seed, float *sink, int32_t blocks, void *stream);
+
+/* Diagnostic: `bytes` from src to dst by the SM-driven copy kernel the serving
+ * loop uses (either side may be pinned host memory); `desc` is 64 bytes of
+ * device scratch for the segment descriptor. */
+int segtaco_probe_copy(void *dst, const void *src, int64_t bytes, void *desc, int32_t blocks,
+                       void *stream);
 
 /* Row-length statistics of a device CSR (the autotuner's input):
  * stats[0] max row length, [1] empty rows, [2] rows >= 32, [3] nonzeros in

@@ -73,7 +73,8 @@ struct SpmmLaunch {
   int rows_per_unit;           // row blocks only
   bool use_tma;                // gather B into a shared-memory ring (spmm_tma.cuh)
   bool bulk_copies;            // ... with cp.async.bulk (TMA) rather than cp.async
-  bool deep;                   // register path: 8 sixteen-byte loads in flight per lane
+  bool deep;                   // row walk: 8 sixteen-byte loads in flight per lane
+  int walk;                    // kWalkRows / kWalkRowsDeep / kWalkFlat (spmm_kernels.cuh)
 };
 // One launcher per (dense type, unit kind); each switches over (V, G).
 int launch_spmm_f32_rows(const SpmmLaunch &L, cudaStream_t s);
@@ -96,6 +97,7 @@ struct SpmmPlan {
   bool use_tma;
   bool bulk_copies;
   bool deep;
+  int walk;                  // kWalkRows / kWalkRowsDeep / kWalkFlat
   size_t workspace;          // bytes
 };
 int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, long long ldc,

@@ -8,29 +8,31 @@
 // per lane in flight, and fold them into one value per warp.  Timing it over
 // buffers smaller and larger than the L2 gives the two ceilings that bound the
 // SpMM kernels.
+#include <algorithm>
+
 #include "common.cuh"
 #include "internal.h"
 
 namespace segtaco {
 namespace {
 
-__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
-  // splitmix64 finaliser (Steele, Lea, Flood 2014)
-  x ^= x >> 30;
-  x *= 0xbf58476d1ce4e5b9ULL;
-  x ^= x >> 27;
-  x *= 0x94d049bb133111ebULL;
-  x ^= x >> 31;
+__device__ __forceinline__ unsigned int mix32(unsigned int x) {
+  // "lowbias32" integer hash (C. Wellons, 2018): two multiplies, three shifts
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
   return x;
 }
 
 template <int LPR>  // lanes per row: row_bytes / 16
-__global__ void __launch_bounds__(256) gather_probe_kernel(const uint4 *__restrict__ buf,
+__global__ void __launch_bounds__(256, 4) gather_probe_kernel(const uint4 *__restrict__ buf,
                                                            long long rows, long long n,
-                                                           unsigned long long seed,
+                                                           unsigned int seed,
                                                            float *__restrict__ sink) {
   constexpr int RPW = 32 / LPR;  // rows per warp step
-  constexpr int U = 4;
+  constexpr int U = 8;
   const int lane = threadIdx.x & 31;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
@@ -41,9 +43,8 @@ __global__ void __launch_bounds__(256) gather_probe_kernel(const uint4 *__restri
     for (int u = 0; u < U; ++u) {
       const long long e = base + u * RPW + lane / LPR;
       if (e < n) {
-        // multiply-high maps the hash uniformly onto [0, rows)
-        const long long r = (long long)__umul64hi(mix64((unsigned long long)e ^ seed),
-                                                  (unsigned long long)rows);
+        // multiply-high maps the 32-bit hash uniformly onto [0, rows)
+        const long long r = (long long)__umulhi(mix32((unsigned int)e ^ seed), (unsigned int)rows);
         v[u] = __ldg(buf + r * LPR + (lane % LPR));
       } else {
         v[u] = make_uint4(0, 0, 0, 0);
@@ -64,21 +65,78 @@ using namespace segtaco;
 
 extern "C" int segtaco_probe_gather(const void *buf, int64_t rows, int32_t row_bytes, int64_t n,
                                     uint32_t seed, float *sink, int32_t blocks, void *stream) {
-  if (!buf || !sink || rows <= 0 || n < 0 || blocks <= 0)
+  if (!buf || !sink || rows <= 0 || n < 0 || blocks < 0)
     return set_error(SEGTACO_EINVAL, "probe: bad arguments");
   if ((reinterpret_cast<uintptr_t>(buf) & 15) != 0)
     return set_error(SEGTACO_EINVAL, "probe: buffer must be 16-byte aligned");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const auto *b = static_cast<const uint4 *>(buf);
-  const unsigned long long sd = 0x9e3779b97f4a7c15ULL * (seed + 1);
+  if (rows > 0xffffffffLL) return set_error(SEGTACO_EINVAL, "probe: at most 2^32 - 1 rows");
+  const unsigned int sd = 0x9e3779b9u * (seed + 1);
+  // blocks == 0: one resident wave (every SM full, no second wave).
+  auto grid = [&](const void *fn) {
+    if (blocks > 0) return blocks;
+    int per_sm = 1, dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, 0);
+    return std::max(1, per_sm) * sms;
+  };
+#define SEGTACO_PROBE(L)                                                       \
+  gather_probe_kernel<L><<<grid((const void *)gather_probe_kernel<L>), 256, 0, s>>>( \
+      b, rows, n, sd, sink);                                                   \
+  break;
   switch (row_bytes) {
-    case 16: gather_probe_kernel<1><<<blocks, 256, 0, s>>>(b, rows, n, sd, sink); break;
-    case 32: gather_probe_kernel<2><<<blocks, 256, 0, s>>>(b, rows, n, sd, sink); break;
-    case 64: gather_probe_kernel<4><<<blocks, 256, 0, s>>>(b, rows, n, sd, sink); break;
-    case 128: gather_probe_kernel<8><<<blocks, 256, 0, s>>>(b, rows, n, sd, sink); break;
-    case 256: gather_probe_kernel<16><<<blocks, 256, 0, s>>>(b, rows, n, sd, sink); break;
-    case 512: gather_probe_kernel<32><<<blocks, 256, 0, s>>>(b, rows, n, sd, sink); break;
+    case 16: SEGTACO_PROBE(1)
+    case 32: SEGTACO_PROBE(2)
+    case 64: SEGTACO_PROBE(4)
+    case 128: SEGTACO_PROBE(8)
+    case 256: SEGTACO_PROBE(16)
+    case 512: SEGTACO_PROBE(32)
     default: return set_error(SEGTACO_EINVAL, "probe: row_bytes must be 16..512, a power of two");
   }
+#undef SEGTACO_PROBE
   return check_launch("gather_probe_kernel");
+}
+
+#include "copy.cuh"
+
+namespace segtaco {
+// The address a kernel uses for `p`: device memory as is, pinned host memory
+// through its mapping; anything else (pageable host memory) is refused, so no
+// kernel ever dereferences memory the GPU cannot reach.
+int device_view(const void *p, void **out) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(SEGTACO_EINVAL, "pointer %p is not known to CUDA", p);
+  }
+  if ((a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged ||
+       a.type == cudaMemoryTypeHost) && a.devicePointer != nullptr) {
+    *out = a.devicePointer;
+    return SEGTACO_OK;
+  }
+  return set_error(SEGTACO_EINVAL, "pointer %p is neither device nor mapped pinned memory", p);
+}
+}  // namespace segtaco
+
+// Diagnostic: one segment moved by copy_segments_kernel (src/dst may be mapped
+// pinned host memory or device memory); the segment descriptor is staged in
+// `desc` (device memory, at least 64 bytes).
+extern "C" int segtaco_probe_copy(void *dst, const void *src, int64_t bytes, void *desc,
+                                  int32_t blocks, void *stream) {
+  using namespace segtaco;
+  if (!dst || !src || !desc || bytes < 0 || blocks <= 0)
+    return set_error(SEGTACO_EINVAL, "probe_copy: bad arguments");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  void *vs = nullptr, *vd = nullptr;
+  SEGTACO_TRY(device_view(src, &vs));
+  SEGTACO_TRY(device_view(dst, &vd));
+  CopySeg sg{static_cast<const char *>(vs), static_cast<char *>(vd), bytes, 0};
+  SEGTACO_TRY(check_cuda(cudaMemcpyAsync(desc, &sg, sizeof(sg), cudaMemcpyHostToDevice, s),
+                         "probe_copy descriptor"));
+  const long long chunks = copy_chunks(bytes);
+  if (chunks == 0) return SEGTACO_OK;
+  copy_segments_kernel<<<blocks, 256, 0, s>>>(static_cast<const CopySeg *>(desc), 1, chunks);
+  return check_launch("copy_segments_kernel");
 }

@@ -261,16 +261,226 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
   }
 }
 
-// DEEP = false: 4 CTAs (32 warps) per SM, at most 64 registers; sixteen-byte
-// vectors keep 4 loads in flight per lane (the bf16 x 8 variants need a few
-// more registers for their 8 accumulators and run 3 CTAs per SM).
-// DEEP = true: 8 loads in flight per lane at 3 CTAs (24 warps) per SM.
-template <typename BT, int V, int G, bool ROWS, bool DEEP = false>
-__global__ void __launch_bounds__(kCta, (V == 8 || DEEP) ? 3 : 4)
+// Flat walk of one unit: the unit's nonzeros in batches of up to 32 (one per
+// lane), each batch inside a window of 32 consecutive rows (lane i holds the
+// end of row wb + i).  Slot s owns batch positions s*Q .. s*Q+Q-1 (Q = G) and
+// sums them in order into `acc`, issuing all of its B loads of a sub-block (up
+// to 8 per lane) before the first multiply-add, whatever the row lengths.  At
+// a position that ends a row the slot writes its sum, except the first row end
+// of slots s >= 1, whose row began in an earlier slot: that partial waits for
+// a segmented scan over the slots (flag = the slot saw a row end, value = the
+// slot's open sum), which also yields the carry of the row still open after
+// the batch.  Slot 0 starts each batch from that carry, so with one slot
+// (P = 1) every row is one sequential fmaf chain in storage order.  Empty rows
+// of the unit are zeroed first, P rows at a time.
+template <typename BT, int V, int G, bool ROWS>
+__device__ __forceinline__ void spmm_flat_unit(const SpmmArgs<BT> &a, long long w, int slab,
+                                               int lane) {
+  constexpr int P = 32 / G;  // slots
+  constexpr int Q = G;       // batch positions per slot
+  constexpr int U = Q < 8 ? Q : 8;
+  using D = Dense<BT, V>;
+  const unsigned FULL = 0xffffffffu;
+  const int slot = lane / G, gl = lane & (G - 1);
+  const int M = a.M;
+  const int col0 = slab * (G * V) + gl * V;
+  const bool active = col0 < a.N;
+  const uint64_t pol = l2_policy(a.l2_hints);
+  const BT *Bc = a.B + (active ? col0 : 0);  // lanes past N load column 0, never store
+  const unsigned ldb = (unsigned)a.ldb;
+
+  int x0, x1, y0, y1, rp0;
+  bool head_split = false, tail_open = false;
+  if (ROWS) {
+    const long long r0 = w * a.rows_per_unit;
+    x0 = (int)r0;
+    x1 = (int)min(r0 + a.rows_per_unit, (long long)M);
+    y0 = rp0 = __ldg(a.row_ptr + x0);
+    y1 = __ldg(a.row_ptr + x1);
+  } else {
+    x0 = __ldg(a.part_x + w);
+    y0 = __ldg(a.part_y + w);
+    x1 = __ldg(a.part_x + w + 1);
+    y1 = __ldg(a.part_y + w + 1);
+    rp0 = x0 < M ? __ldg(a.row_ptr + x0) : y0;
+    head_split = rp0 < y0;
+    tail_open = x1 < M && __ldg(a.row_ptr + x1) < y1;
+  }
+  const int last = tail_open ? x1 : x1 - 1;  // rows of this unit: x0 .. last
+  // Window: lane i holds the end of row wb + i (INT_MAX past M).
+  auto window = [&](int base) {
+    return (base + lane < M) ? __ldg(a.row_ptr + base + 1 + lane) : INT_MAX;
+  };
+  int wb = x0;
+  int rw = window(wb);
+  int p0 = y0;
+  int mc = lane < y1 - p0 ? ld_stream(a.col + p0 + lane) : 0;
+  float mv = lane < y1 - p0 ? ld_val(a.val, p0 + lane) : 0.0f;
+  float acc[V], head[V];
+  zero<V>(acc);
+  zero<V>(head);
+
+  // ---- empty rows of the unit (row starts from the window) ----
+  {
+    int e = rw, before = rp0;
+    for (int rb = x0; rb <= last; rb += 32) {
+      if (rb != x0) e = window(rb);
+      int sb = __shfl_up_sync(FULL, e, 1);
+      if (lane == 0) sb = before;
+      const bool empty = rb + lane <= last && e == sb;
+      before = __shfl_sync(FULL, e, 31);
+      unsigned m = __ballot_sync(FULL, empty);
+      while (m) {  // slot s zeroes the s-th remaining empty row
+        unsigned mm = m;
+        int pos = -1;
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+          const int b = __ffs(mm) - 1;
+          if (q == slot) pos = b;
+          mm &= mm - 1;
+        }
+        if (pos >= 0 && active) store_c<V>(a.C + (long long)(rb + pos) * a.ldc + col0, acc);
+        m = mm;
+      }
+    }
+  }
+
+  // ---- nonzeros ----
+  while (p0 < y1) {
+    // The window must start at or before the row of p0 and contain it.
+    int wend = __shfl_sync(FULL, rw, 31);
+    while (wend <= p0) {  // every window row ends by p0: move on 32 rows
+      wb += 32;
+      rw = window(wb);
+      wend = __shfl_sync(FULL, rw, 31);
+    }
+    // Batch: nonzeros p0 .. pe-1, all in rows of the window.
+    int pe = p0 + 32;
+    if (pe > y1) pe = y1;
+    if (pe > wend) pe = wend;
+    const int nb = pe - p0;
+    const int mcn = lane < y1 - pe ? ld_stream(a.col + pe + lane) : 0;
+    const float mvn = lane < y1 - pe ? ld_val(a.val, pe + lane) : 0.0f;
+    // Window row of nonzero p0 + lane: the number of window rows ending <= it.
+    const int p = p0 + lane;
+    int rr = 0;
+#pragma unroll
+    for (int st = 16; st > 0; st >>= 1) {
+      const int cand = __shfl_sync(FULL, rw, rr + st - 1);
+      if (cand <= p) rr += st;
+    }
+    const int rend = __shfl_sync(FULL, rw, rr);
+    // code: bit 0 = ends its row (valid positions only), bits 2.. = window row
+    const int code = lane < nb ? (rr << 2) | (rend == p + 1 ? 1 : 0) : 0;
+
+    if (slot != 0) zero<V>(acc);
+    bool flushed = false;
+    int hrow = 0;
+    const int kend = nb < Q ? nb : Q;  // slot 0 holds the most valid positions
+    // Sub-blocks of U positions, one after another (unrolling them would let
+    // the compiler hoist every load of the batch and spill).
+#pragma unroll 1
+    for (int k0 = 0; k0 < kend; k0 += U) {
+      typename D::raw_t b[U];
+      // Positions past the batch (t >= nb) reload the batch's first B row
+      // (a cache hit, no new traffic) and are never used.
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int t = slot * Q + k0 + u;
+        const int j = __shfl_sync(FULL, mc, t < nb ? t : 0);
+        b[u] = D::load(Bc + (size_t)(unsigned)j * ldb, pol);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int t = slot * Q + k0 + u;
+        const float x = __shfl_sync(FULL, mv, t);
+        const int cd = __shfl_sync(FULL, code, t);
+        if (t < nb) {
+#pragma unroll
+          for (int v = 0; v < V; ++v) acc[v] = fmaf(x, D::get(b[u], v), acc[v]);
+        }
+        if (cd & 1) {
+          const int row = wb + (cd >> 2);
+          if (slot == 0 || flushed) {
+            if (active) {
+              float *dst = a.C + (long long)row * a.ldc + col0;
+              if (!ROWS && ((row == x0 && head_split) || (row == x1 && tail_open)))
+                atomic_add_c<V>(dst, acc);
+              else
+                store_c<V>(dst, acc);
+            }
+          } else {
+#pragma unroll
+            for (int v = 0; v < V; ++v) head[v] = acc[v];
+            hrow = row;
+          }
+          flushed = true;
+          zero<V>(acc);
+        }
+      }
+    }
+    if (P > 1) {
+      // Inclusive segmented scan over slots: value = open sum, reset where a
+      // slot saw a row end.
+      float sc[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) sc[v] = acc[v];
+      int f = flushed ? 1 : 0;
+#pragma unroll
+      for (int d = 1; d < P; d <<= 1) {
+        const int fo = __shfl_up_sync(FULL, f, d * G);
+        float o[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) o[v] = __shfl_up_sync(FULL, sc[v], d * G);
+        if (slot >= d) {
+          if (!f) {
+#pragma unroll
+            for (int v = 0; v < V; ++v) sc[v] += o[v];
+          }
+          f |= fo;
+        }
+      }
+      // The first row end of slot s >= 1 closes the row open after slot s-1.
+      float in[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) in[v] = __shfl_up_sync(FULL, sc[v], G);
+      if (slot > 0 && flushed && active) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) head[v] += in[v];
+        float *dst = a.C + (long long)hrow * a.ldc + col0;
+        if (!ROWS && ((hrow == x0 && head_split) || (hrow == x1 && tail_open)))
+          atomic_add_c<V>(dst, head);
+        else
+          store_c<V>(dst, head);
+      }
+      // Carry of the row still open: the scan value of the last slot, to slot 0.
+#pragma unroll
+      for (int v = 0; v < V; ++v) acc[v] = __shfl_sync(FULL, sc[v], (P - 1) * G + gl);
+    }
+    p0 = pe;
+    mc = mcn;
+    mv = mvn;
+  }
+  // The row open at the unit's end continues in the next unit (tail_open).
+  if (!ROWS && tail_open && slot == 0 && active)
+    atomic_add_c<V>(a.C + (long long)x1 * a.ldc + col0, acc);
+}
+
+// Walks of a unit: the row walk with 4 or 8 loads in flight per lane, or the
+// flat walk (chosen by the planner, api.cu).
+constexpr int kWalkRows = 0, kWalkRowsDeep = 1, kWalkFlat = 2;
+
+// 4 CTAs (32 warps) per SM at most 64 registers; the bf16 x 8 variants and the
+// deep row walk need more registers and run 3 CTAs per SM.
+template <typename BT, int V, int G, bool ROWS, int WALK = kWalkRows>
+__global__ void __launch_bounds__(kCta, (V == 8 || WALK == kWalkRowsDeep) ? 3 : 4)
     spmm_seg_kernel(SpmmArgs<BT> a) {
   const long long w = (long long)blockIdx.x * (kCta / 32) + threadIdx.x / 32;
   if (w >= a.units) return;  // whole warp leaves together
-  spmm_walk_unit<BT, V, G, ROWS, DEEP>(a, w, blockIdx.y, threadIdx.x & 31);
+  if (WALK == kWalkFlat)
+    spmm_flat_unit<BT, V, G, ROWS>(a, w, blockIdx.y, threadIdx.x & 31);
+  else
+    spmm_walk_unit<BT, V, G, ROWS, WALK == kWalkRowsDeep>(a, w, blockIdx.y, threadIdx.x & 31);
 }
 
 }  // namespace segtaco

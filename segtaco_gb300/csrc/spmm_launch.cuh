@@ -48,14 +48,16 @@ inline dim3 spmm_grid(const SpmmLaunch &L) {
 #define SEGTACO_VG_BF16(X, R) \
   SEGTACO_VG_F32(X, R) X(8, 1, R) X(8, 2, R) X(8, 4, R) X(8, 8, R) X(8, 16, R) X(8, 32, R)
 
-// Sixteen-byte-vector variants with 8 loads in flight per lane.
-#define SEGTACO_DEEP_CASE(BT, G, R) \
-  case G:                           \
-    spmm_seg_kernel<BT, 16 / sizeof(BT), G, R, true><<<grid, kCta, 0, s>>>(a); \
+// Sixteen-byte-vector variants of the other walks: the row walk with 8 loads
+// in flight per lane (kWalkRowsDeep) and the flat walk (kWalkFlat).
+#define SEGTACO_WALK_CASE(BT, G, R, WALK) \
+  case G:                                 \
+    spmm_seg_kernel<BT, 16 / sizeof(BT), G, R, WALK><<<grid, kCta, 0, s>>>(a); \
     break;
-#define SEGTACO_DEEP_CASES(BT, R)                                             \
-  SEGTACO_DEEP_CASE(BT, 1, R) SEGTACO_DEEP_CASE(BT, 2, R) SEGTACO_DEEP_CASE(BT, 4, R) \
-  SEGTACO_DEEP_CASE(BT, 8, R) SEGTACO_DEEP_CASE(BT, 16, R) SEGTACO_DEEP_CASE(BT, 32, R)
+#define SEGTACO_WALK_CASES(BT, R, WALK)                                                 \
+  SEGTACO_WALK_CASE(BT, 1, R, WALK) SEGTACO_WALK_CASE(BT, 2, R, WALK)                   \
+  SEGTACO_WALK_CASE(BT, 4, R, WALK) SEGTACO_WALK_CASE(BT, 8, R, WALK)                   \
+  SEGTACO_WALK_CASE(BT, 16, R, WALK) SEGTACO_WALK_CASE(BT, 32, R, WALK)
 
 // Defines int NAME(const SpmmLaunch&, cudaStream_t) for one (dtype, unit kind).
 #define SEGTACO_DEFINE_SPMM_LAUNCHER(NAME, BT, VG_LIST, ROWS)                             \
@@ -63,11 +65,19 @@ inline dim3 spmm_grid(const SpmmLaunch &L) {
   int NAME(const SpmmLaunch &L, cudaStream_t s) {                                         \
     const SpmmArgs<BT> a = make_spmm_args<BT>(L);                                         \
     const dim3 grid = spmm_grid(L);                                                       \
-    if (L.deep && L.V * (int)sizeof(BT) == 16) {                                          \
-      switch (L.G) {                                                                      \
-        SEGTACO_DEEP_CASES(BT, ROWS)                                                      \
-        default:                                                                          \
-          return set_error(SEGTACO_EUNSUPPORTED, #NAME ": no deep variant G=%d", L.G);     \
+    if (L.walk != kWalkRows && L.V * (int)sizeof(BT) == 16) {                            \
+      if (L.walk == kWalkRowsDeep) {                                                      \
+        switch (L.G) {                                                                    \
+          SEGTACO_WALK_CASES(BT, ROWS, kWalkRowsDeep)                                     \
+          default:                                                                        \
+            return set_error(SEGTACO_EUNSUPPORTED, #NAME ": no deep walk G=%d", L.G);      \
+        }                                                                                 \
+      } else {                                                                            \
+        switch (L.G) {                                                                    \
+          SEGTACO_WALK_CASES(BT, ROWS, kWalkFlat)                                         \
+          default:                                                                        \
+            return set_error(SEGTACO_EUNSUPPORTED, #NAME ": no flat walk G=%d", L.G);      \
+        }                                                                                 \
       }                                                                                   \
       return check_launch(#NAME);                                                         \
     }                                                                                     \

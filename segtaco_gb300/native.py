@@ -35,6 +35,8 @@ FLAG_L2_HINTS = 1
 FLAG_PARTITION_READY = 2
 FLAG_SMEM_RING = 4
 FLAG_TMA_BULK = 8
+FLAG_ROW_WALK = 16
+FLAG_FLAT_WALK = 32
 
 
 class SegtacoError(RuntimeError):
@@ -144,6 +146,7 @@ SIGNATURES = {
     "segtaco_server_get_stats": (C.c_int, [_P, _I, C.POINTER(ServerStats)]),
     "segtaco_server_destroy": (C.c_int, [_P]),
     "segtaco_probe_gather": (C.c_int, [_P, _I64, _I, _I64, C.c_uint32, _P, _I, _P]),
+    "segtaco_probe_copy": (C.c_int, [_P, _P, _I64, _P, _I, _P]),
     "segtaco_block_starts_taco": (C.c_int, [_I, _I64, _P, _I, _P, _P]),
     "segtaco_block_starts_canonical": (C.c_int, [_I, _I64, _P, _I, _P, _P]),
     "segtaco_merge_path": (C.c_int, [_I, _I64, _P, _I64, _P, _P, _P]),

@@ -111,6 +111,10 @@ def test_argument_errors_without_device(native_lib):
     st = L.segtaco_spmm(4, 4, 0, C.c_void_p(256), C.c_void_p(256), None, C.c_void_p(256), N.F32,
                         4, C.c_void_p(256), 4, 4, C.byref(bad), None, 0, None)
     assert st == N.EINVAL and "schedule" in N.last_error()
+    both = N.Config.make(flags=N.FLAG_ROW_WALK | N.FLAG_FLAT_WALK)
+    st = L.segtaco_spmm(4, 4, 0, C.c_void_p(256), C.c_void_p(256), None, C.c_void_p(256), N.F32,
+                        4, C.c_void_p(256), 4, 4, C.byref(both), None, 0, None)
+    assert st == N.EINVAL and "exclusive" in N.last_error()
     assert L.segtaco_taco_call(b"no_such_kernel", None, None, None, None) == N.EINVAL
 
 

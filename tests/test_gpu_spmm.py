@@ -13,9 +13,10 @@ from segtaco_gb300 import ops, synth
 
 pytestmark = pytest.mark.gpu
 SCHEDULES = ["rb_sr", "rb_pr", "eb_sr", "eb_pr"]
-# How B rows are gathered: register loads (default), cp.async into a
-# shared-memory ring, or TMA bulk copies into the ring.
-PATHS = {"regs": 0, "ring": N.FLAG_SMEM_RING, "bulk": N.FLAG_SMEM_RING | N.FLAG_TMA_BULK}
+# How a unit is walked and B rows gathered: the planner's choice, the flat
+# walk, the row walk, cp.async into a shared-memory ring, or TMA bulk copies.
+PATHS = {"auto": 0, "flat": N.FLAG_FLAT_WALK, "rows": N.FLAG_ROW_WALK,
+         "ring": N.FLAG_SMEM_RING, "bulk": N.FLAG_SMEM_RING | N.FLAG_TMA_BULK}
 SMALL = small_cases()
 
 
@@ -65,7 +66,8 @@ def test_tuning_knobs(cuda, sched):
     B = synth.dense(A.K, 64, seed=5)
     ref = spmm_ref(A, B)
     for col_tile in (4, 16, 32, 64, 128):
-        for vec, flags in ((1, 0), (2, 0), (4, 0), (4, N.FLAG_SMEM_RING)):
+        for vec, flags in ((1, 0), (2, 0), (4, 0), (4, N.FLAG_ROW_WALK), (4, N.FLAG_FLAT_WALK),
+                           (4, N.FLAG_SMEM_RING)):
             for units in (1, 3, 7, 64, 1024):
                 kw = dict(schedule=sched, col_tile=col_tile, vec=vec, flags=flags)
                 if sched.startswith("rb"):
