@@ -309,6 +309,96 @@ def run_batched(args, N_, ops, stream, count=256):
     }
 
 
+def _time_events(fn, stream, reps, warm=3):
+    import torch
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def run_side_ops(args, N_, ops, stream, A_pl, peak):
+    """The other hot-path operations at their configurations: SpMV on the
+    power-law matrix (x of 1M fp32), SDDMM with fp32 and bf16 factors of width
+    64 and SpMM with fp32 and bf16 B (N = 64) on the banded-plus-random matrix
+    (262,144^2, ~19.1M nonzeros).  bf16 error: max over 4,096 sampled rows of
+    |c - c64| / sum |a b| against an FP64 product of the same bf16 values."""
+    import numpy as np
+    import torch
+    from segtaco_gb300 import synth
+    reps = max(5, args.steps // 2)
+    out = {}
+    # SpMV, power-law matrix (already resident)
+    Ad = A_pl
+    x = torch.from_numpy(synth.dense(Ad.K, 1, seed=3).ravel()).cuda()
+    y = torch.empty(Ad.M, dtype=torch.float32, device="cuda")
+    ws = torch.empty(max(256, ops.spmv_workspace_size(Ad)), dtype=torch.uint8, device="cuda")
+    ms = _time_events(lambda: ops.spmv(Ad, x, y, workspace=ws, stream=stream), stream, reps)
+    byts = Ad.nnz * 8 + (Ad.M + 1) * 4 + Ad.K * 4 + Ad.M * 4
+    out["spmv_power_law"] = {"ms": round(ms, 4), "GBps": round(byts / ms / 1e6, 1),
+                             "roofline_frac": round(byts / ms / 1e6 / peak, 4),
+                             "bytes": byts}
+    # banded-plus-random: SDDMM and SpMM, fp32 and bf16 dense operands
+    A = synth.banded_plus_random(seed=0)
+    Bd = ops.DeviceCSR.from_host(A, "cuda")
+    D = 64
+    X32 = synth.dense(A.M, D, seed=4)
+    Y32 = synth.dense(A.K, D, seed=5)
+    o = torch.empty(A.nnz, dtype=torch.float32, device="cuda")
+    for name, conv, esz in (("f32", lambda a: torch.from_numpy(a).cuda(), 4),
+                            ("bf16", lambda a: torch.from_numpy(synth.to_bf16_bits(a).view(np.int16))
+                             .cuda().view(torch.bfloat16), 2)):
+        X, Y = conv(X32), conv(Y32)
+        ms = _time_events(lambda: ops.sddmm(Bd, X, Y, o, stream=stream), stream, reps)
+        byts = A.nnz * 12 + (A.M + 1) * 4 + (A.M + A.K) * D * esz
+        out["sddmm_banded_" + name] = {"ms": round(ms, 4), "GBps": round(byts / ms / 1e6, 1),
+                                       "roofline_frac": round(byts / ms / 1e6 / peak, 4),
+                                       "bytes": byts}
+        Bm = conv(synth.dense(A.K, D, seed=6))
+        Cm = torch.empty((A.M, D), dtype=torch.float32, device="cuda")
+        cfg = N_.Config.make(schedule=N_.AUTO)
+        N_.check(N_.lib().segtaco_autotune_heuristic(A.M, A.K, A.nnz, D,
+                                                    N_.F32 if esz == 4 else N_.BF16,
+                                                    int(A.row_lengths().max()), cfg))
+        wsz = max(256, ops.spmm_workspace_size(Bd, D, N_.F32 if esz == 4 else N_.BF16, cfg))
+        w = torch.empty(wsz, dtype=torch.uint8, device="cuda")
+        ms = _time_events(lambda: ops.spmm(Bd, Bm, C_out=Cm, config=cfg, workspace=w,
+                                           stream=stream), stream, reps)
+        byts = algorithmic_bytes(A.M, A.K, A.nnz, D, esz)
+        ent = {"ms": round(ms, 4), "GBps": round(byts / ms / 1e6, 1),
+               "roofline_frac": round(byts / ms / 1e6 / peak, 4), "bytes": byts,
+               "schedule": {v: k for k, v in N_.SCHEDULES.items()}[cfg.schedule]}
+        if esz == 2:
+            # error of the bf16-B product against FP64 over sampled rows
+            torch.cuda.synchronize()
+            rng = np.random.default_rng(7)
+            rows = np.sort(rng.choice(A.M, 4096, replace=False))
+            Bh = Bm.view(torch.int16).cpu().numpy().view(np.uint16)
+            Bf = synth.bf16_bits_to_f32(Bh).astype(np.float64)
+            Ch = Cm.cpu().numpy()
+            worst = 0.0
+            for r in rows:
+                s0, s1 = A.row_ptr[r], A.row_ptr[r + 1]
+                a = A.val[s0:s1].astype(np.float64)
+                rowsB = Bf[A.col[s0:s1]]
+                exact = a @ rowsB
+                bound = np.abs(a) @ np.abs(rowsB)
+                err = np.abs(Ch[r] - exact) / np.maximum(bound, 1e-30)
+                worst = max(worst, float(err.max()))
+            ent["max_err_vs_fp64_bf16_values"] = worst
+            ent["tolerance"] = 1e-5
+        out["spmm_banded_" + name] = ent
+    out["config"] = "SpMV: power-law 1Mx1M (%d nnz); banded-plus-random %dx%d, %d nnz, D=N=64" % (
+        Ad.nnz, A.M, A.K, A.nnz)
+    return out
+
+
 def run_gather_ceiling(ops, stream, reps=5):
     """Random-row gather throughput of this GPU (segtaco_probe_gather) over
     buffers that fit in L2 and buffers that do not: the ceilings that bound
@@ -553,6 +643,9 @@ def run_ours(args, world, rank, local):
     served = None
     if not args.no_serving:
         served = run_serving(args, N_)
+    side = None
+    if not args.no_side_ops:
+        side = run_side_ops(args, N_, ops, stream, Ad, peak)
     ceiling = None
     if not args.no_probe:
         ceiling = run_gather_ceiling(ops, stream)
@@ -586,7 +679,7 @@ def run_ours(args, world, rank, local):
             "gpu_launches": args.steps * (2 if eb else 1),
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks, "schedules": schedules,
             "vendor": vendor, "batched": batched, "served": served,
-            "gather_ceiling": ceiling,
+            "gather_ceiling": ceiling, "side_ops": side,
         }
         print(json.dumps(line), flush=True)
 
@@ -612,6 +705,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-probe", action="store_true")
+    ap.add_argument("--no-side-ops", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup(args)

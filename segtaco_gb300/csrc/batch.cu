@@ -256,7 +256,7 @@ int batch_image(const segtaco_spmm_problem *probs, const SpmmPlan *plans, int co
     // Persistent grid: every SM full, never more CTAs than the items need.
     int per_sm = 0;
     SEGTACO_TRY(blocks_per_sm(device, g.dtype, g.V, g.G, g.rows, &per_sm));
-    const long long need = (item + (kCta / 32) - 1) / (kCta / 32);
+    const long long need = (item + kSpmmWarps - 1) / kSpmmWarps;
     long long grid = (long long)std::max(1, per_sm) * std::max(1, sms);
     if (grid > need) grid = std::max(1LL, need);
     g.grid = (int)grid;

@@ -7,14 +7,14 @@ namespace segtaco {
 
 #define SEGTACO_BATCH_CASE(V, G, R)                                                        \
   case V * 100 + G:                                                                        \
-    spmm_batch_kernel<uint16_t, V, G, R><<<g.grid, kCta, 0, s>>>(                            \
+    spmm_batch_kernel<uint16_t, V, G, R><<<g.grid, kSpmmCta, 0, s>>>(                            \
         static_cast<const BatchProblem<uint16_t> *>(g.probs), g.item_begin, g.nprobs,         \
         g.total_items, g.queue, g.gate);                                                           \
     break;
 #define SEGTACO_BATCH_OCC(V, G, R)                                                         \
   case V * 100 + G:                                                                        \
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, spmm_batch_kernel<uint16_t, V, G, R>, \
-                                                      kCta, 0);                            \
+                                                      kSpmmCta, 0);                            \
     break;
 
 int launch_batch_bf16(const BatchGroupLaunch &g, cudaStream_t s) {

@@ -470,12 +470,20 @@ __device__ __forceinline__ void spmm_flat_unit(const SpmmArgs<BT> &a, long long 
 // flat walk (chosen by the planner, api.cu).
 constexpr int kWalkRows = 0, kWalkRowsDeep = 1, kWalkFlat = 2;
 
-// 4 CTAs (32 warps) per SM at most 64 registers; the bf16 x 8 variants and the
-// deep row walk need more registers and run 3 CTAs per SM.
+// CTAs of the SpMM kernels: 4 warps each, so a CTA that finishes early frees
+// its slot soon (warps of a CTA walk units of uneven cost).  32 warps per SM
+// at most 64 registers; the bf16 x 8 variants and the deep row walk need more
+// registers and run 24.
+constexpr int kSpmmCta = 128;
+constexpr int kSpmmWarps = kSpmmCta / 32;
+template <int V, bool HEAVY> constexpr int spmm_min_ctas() {
+  return ((V == 8 || HEAVY) ? 24 : 32) / kSpmmWarps;
+}
+
 template <typename BT, int V, int G, bool ROWS, int WALK = kWalkRows>
-__global__ void __launch_bounds__(kCta, (V == 8 || WALK == kWalkRowsDeep) ? 3 : 4)
+__global__ void __launch_bounds__(kSpmmCta, spmm_min_ctas<V, WALK == kWalkRowsDeep>())
     spmm_seg_kernel(SpmmArgs<BT> a) {
-  const long long w = (long long)blockIdx.x * (kCta / 32) + threadIdx.x / 32;
+  const long long w = (long long)blockIdx.x * kSpmmWarps + threadIdx.x / 32;
   if (w >= a.units) return;  // whole warp leaves together
   if (WALK == kWalkFlat)
     spmm_flat_unit<BT, V, G, ROWS>(a, w, blockIdx.y, threadIdx.x & 31);

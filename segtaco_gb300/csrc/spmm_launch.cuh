@@ -34,7 +34,7 @@ template <typename BT> inline SpmmArgs<BT> make_spmm_args(const SpmmLaunch &L) {
 inline dim3 spmm_grid(const SpmmLaunch &L) {
   const long long W = (long long)L.V * L.G;
   const unsigned slabs = (unsigned)((L.N + W - 1) / W);
-  long long x = (L.units + (kCta / 32) - 1) / (kCta / 32);
+  long long x = (L.units + kSpmmWarps - 1) / kSpmmWarps;
   if (x < 1) x = 1;
   return dim3((unsigned)x, slabs, 1);
 }
@@ -52,7 +52,7 @@ inline dim3 spmm_grid(const SpmmLaunch &L) {
 // in flight per lane (kWalkRowsDeep) and the flat walk (kWalkFlat).
 #define SEGTACO_WALK_CASE(BT, G, R, WALK) \
   case G:                                 \
-    spmm_seg_kernel<BT, 16 / sizeof(BT), G, R, WALK><<<grid, kCta, 0, s>>>(a); \
+    spmm_seg_kernel<BT, 16 / sizeof(BT), G, R, WALK><<<grid, kSpmmCta, 0, s>>>(a); \
     break;
 #define SEGTACO_WALK_CASES(BT, R, WALK)                                                 \
   SEGTACO_WALK_CASE(BT, 1, R, WALK) SEGTACO_WALK_CASE(BT, 2, R, WALK)                   \

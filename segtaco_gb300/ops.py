@@ -109,11 +109,22 @@ def spmm_partition(A: DeviceCSR, C_out: torch.Tensor, config: N.Config, workspac
                                            _stream(stream)))
 
 
-def spmv(A: DeviceCSR, x: torch.Tensor, y: torch.Tensor | None = None, stream=None):
+def spmv_workspace_size(A: DeviceCSR) -> int:
+    out = C.c_size_t()
+    N.check(N.lib().segtaco_spmv_workspace_size(A.M, A.nnz, C.byref(out)))
+    return out.value
+
+
+def spmv(A: DeviceCSR, x: torch.Tensor, y: torch.Tensor | None = None,
+         workspace: torch.Tensor | None = None, stream=None):
+    """y = A @ x (fp32)."""
     if y is None:
         y = torch.empty(A.M, dtype=torch.float32, device=x.device)
+    ws_ptr, ws_bytes = None, 0
+    if workspace is not None:
+        ws_ptr, ws_bytes = _ptr(workspace), workspace.numel() * workspace.element_size()
     N.check(N.lib().segtaco_spmv(A.M, A.K, A.nnz, _ptr(A.row_ptr), _ptr(A.col), _ptr(A.val),
-                                 _ptr(x), _ptr(y), None, 0, _stream(stream)))
+                                 _ptr(x), _ptr(y), ws_ptr, ws_bytes, _stream(stream)))
     return y
 
 
