@@ -274,6 +274,30 @@ int segtaco_probe_gather(const void *buf, int64_t rows, int32_t row_bytes, int64
 int segtaco_probe_copy(void *dst, const void *src, int64_t bytes, void *desc, int32_t blocks,
                        void *stream);
 
+/* ---- MatrixMarket ingest (host) ------------------------------------------ */
+#define SEGTACO_MTX_SEGTACO_PATTERN 1u /* the CSR segTACO's read_mtx_file builds
+                                          (symmetric files mirrored, sorted and
+                                          deduplicated, then cut to the header's
+                                          entry count; others sorted, duplicates
+                                          kept); default: all symmetries mirrored,
+                                          duplicates summed                     */
+#define SEGTACO_MTX_VALUES_FILE 0      /* values from the file (pattern: 1)     */
+#define SEGTACO_MTX_VALUES_SEGTACO 1   /* {0, 0.1, 0.2} like segTACO's
+                                          fill_random, from a seeded generator  */
+#define SEGTACO_MTX_VALUES_ONES 2
+
+typedef struct segtaco_host_csr {
+  int32_t M, K;
+  int64_t nnz;
+  int32_t *row_ptr, *col; /* malloc'd; free with segtaco_host_csr_free */
+  float *vals;
+} segtaco_host_csr;
+/* Reads a MatrixMarket coordinate file into a host CSR (columns sorted within
+ * rows).  Replaces segTACO's read_mtx_file + fill_random (ds.h:183-274). */
+int segtaco_mtx_read(const char *path, uint32_t flags, int32_t values, uint64_t seed,
+                     segtaco_host_csr *out);
+void segtaco_host_csr_free(segtaco_host_csr *csr);
+
 /* Row-length statistics of a device CSR (the autotuner's input):
  * stats[0] max row length, [1] empty rows, [2] rows >= 32, [3] nonzeros in
  * rows >= 32.  Synchronises `stream`. */

@@ -46,21 +46,32 @@ def _compile(src, obj, extra):
     return r.stderr
 
 
+def _compile_host(src, obj, extra):
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-I", INCLUDE, "-I", CSRC,
+           "-I", os.path.join(os.path.dirname(os.path.dirname(nvcc())), "include"),
+           "-c", src, "-o", obj]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("g++ failed on %s:\n%s\n%s" % (src, r.stdout, r.stderr))
+    return r.stderr
+
+
 def build(force: bool = False, verbose: bool = False, jobs: int | None = None,
           extra=()) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
     hdr_mtime = max([os.path.getmtime(h) for h in _headers()] + [os.path.getmtime(__file__)])
     todo, objs = [], []
     for s in srcs:
-        o = os.path.join(BUILD, os.path.basename(s)[:-3] + ".o")
+        o = os.path.join(BUILD, os.path.splitext(os.path.basename(s))[0] + ".o")
         objs.append(o)
         if force or not os.path.exists(o) or os.path.getmtime(o) < max(os.path.getmtime(s), hdr_mtime):
             todo.append((s, o))
     if todo:
         jobs = jobs or min(len(todo), max(1, os.cpu_count() or 1))
         with cf.ThreadPoolExecutor(jobs) as ex:
-            futs = {ex.submit(_compile, s, o, list(extra)): s for s, o in todo}
+            futs = {ex.submit(_compile_host if s.endswith(".cpp") else _compile, s, o,
+                              list(extra)): s for s, o in todo}
             for f in cf.as_completed(futs):
                 msg = f.result()
                 if verbose and msg:

@@ -102,6 +102,17 @@ class ServerStats(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+MTX_SEGTACO_PATTERN = 1
+MTX_VALUES_FILE, MTX_VALUES_SEGTACO, MTX_VALUES_ONES = 0, 1, 2
+
+
+class HostCSR(C.Structure):
+    """segtaco_host_csr (arrays malloc'd by the library)."""
+    _fields_ = [("M", C.c_int32), ("K", C.c_int32), ("nnz", C.c_int64),
+                ("row_ptr", C.POINTER(C.c_int32)), ("col", C.POINTER(C.c_int32)),
+                ("vals", C.POINTER(C.c_float))]
+
+
 class TacoTensor(C.Structure):
     """taco_tensor_t (segTACO taco_tensor_t.h:6-15), same layout."""
     _fields_ = [("order", C.c_int32), ("dimensions", C.POINTER(C.c_int32)),
@@ -147,6 +158,8 @@ SIGNATURES = {
     "segtaco_server_destroy": (C.c_int, [_P]),
     "segtaco_probe_gather": (C.c_int, [_P, _I64, _I, _I64, C.c_uint32, _P, _I, _P]),
     "segtaco_probe_copy": (C.c_int, [_P, _P, _I64, _P, _I, _P]),
+    "segtaco_mtx_read": (C.c_int, [C.c_char_p, C.c_uint32, _I, C.c_uint64, C.POINTER(HostCSR)]),
+    "segtaco_host_csr_free": (None, [C.POINTER(HostCSR)]),
     "segtaco_block_starts_taco": (C.c_int, [_I, _I64, _P, _I, _P, _P]),
     "segtaco_block_starts_canonical": (C.c_int, [_I, _I64, _P, _I, _P, _P]),
     "segtaco_merge_path": (C.c_int, [_I, _I64, _P, _I64, _P, _P, _P]),

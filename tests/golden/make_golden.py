@@ -12,6 +12,8 @@ It builds oracle/_ref (oracle/build.py), feeds the seeded inputs below to
 * ``ref_golden spmv``  -> Eigen ``EigenCSR * EigenVector``
 * ``ref_golden sddmm`` -> ``sddmm_csr_cpu_taco_ref`` (sddmm_csr_gpu.h:9-50), in double
 * ``ref_golden csr``   -> ``to_eigen_csr`` (ds.h:380-397) on an unsorted COO
+* ``ref_golden mtx``   -> ``read_mtx_file`` (ds.h:183-268) on the MatrixMarket
+                          texts of ``mtx_texts()``
 * ``ref_search``       -> ``taco_binarySearchBefore/After`` (gpu_library.h:164-205)
                           and the block-start rule of gpu_library.h:206-240
 
@@ -45,6 +47,37 @@ def _write(path, *arrays):
 
 def _run(binary, *args):
     subprocess.run([binary, *args], check=True)
+
+
+def mtx_texts():
+    """MatrixMarket files covering the reader's branches (all entries valid;
+    none where deduplication would leave fewer coordinates than the header
+    declares, on which segTACO's reader reads past its list)."""
+    rng = np.random.default_rng(41)
+    t = {}
+    # general real: unsorted entries, a duplicate, comments and a blank line
+    ent = [(3, 1, 0.5), (1, 2, -1.0), (2, 2, 2.0), (1, 2, 3.0), (4, 4, 1.5), (1, 1, 7.0)]
+    t["general_real"] = ("%%MatrixMarket matrix coordinate real general\n% comment\n\n4 5 6\n" +
+                         "".join("%d %d %g\n" % e for e in ent))
+    # symmetric pattern with diagonal entries (lower triangle stored)
+    pairs = sorted({(int(i), int(j)) for i, j in rng.integers(1, 31, (60, 2)) if i >= j})
+    t["symmetric_pattern"] = ("%%MatrixMarket matrix coordinate pattern symmetric\n" +
+                              "30 30 %d\n" % len(pairs) + "".join("%d %d\n" % p for p in pairs))
+    # symmetric real: mirroring exceeds the header count (the cut applies)
+    pairs = sorted({(int(i), int(j)) for i, j in rng.integers(1, 41, (120, 2)) if i > j})
+    t["symmetric_real_cut"] = ("%%MatrixMarket matrix coordinate real symmetric\n" +
+                               "40 40 %d\n" % len(pairs) +
+                               "".join("%d %d %.3f\n" % (i, j, (i + j) / 10) for i, j in pairs))
+    # skew-symmetric and hermitian (segTACO treats both as general)
+    t["skew_real"] = ("%%MatrixMarket matrix coordinate real skew-symmetric\n5 5 3\n"
+                      "2 1 1.0\n4 3 -2.0\n5 1 0.5\n")
+    t["hermitian_complex"] = ("%%MatrixMarket matrix coordinate complex hermitian\n4 4 4\n"
+                              "1 1 1.0 0.0\n3 1 2.0 1.0\n4 2 -1.0 0.5\n4 4 3.0 0.0\n")
+    # integer, CRLF line ends, a column-only tail
+    t["integer_crlf"] = ("%%MatrixMarket matrix coordinate integer general\r\n3 7 4\r\n"
+                         "1 7 5\r\n3 1 -2\r\n2 4 9\r\n3 7 1\r\n")
+    t["empty"] = "%%MatrixMarket matrix coordinate real general\n6 3 0\n"
+    return t
 
 
 def spmm_cases():
@@ -144,6 +177,21 @@ def main():
     val = r[M + 1 + nnz:].view(np.float32)
     np.savez_compressed(os.path.join(HERE, "csr_from_coo.npz"), M=M, K=K, rows=rows, cols=cols,
                         vals=vals, row_ptr=rp, col=col, val=val)
+    # ---- MatrixMarket reading -----------------------------------------------
+    rec = {}
+    for name, text in mtx_texts().items():
+        path = os.path.join(tmp, name + ".mtx")
+        with open(path, "w", newline="") as f:
+            f.write(text)
+        _run(g, "mtx", path, fout)
+        raw = open(fout, "rb").read()
+        nrow, ncol, nnz = np.frombuffer(raw[:24], np.int64)
+        ints = np.frombuffer(raw[24:], np.int32)
+        rec["text_" + name] = np.frombuffer(text.encode(), np.uint8)
+        rec["shape_" + name] = np.array([nrow, ncol, nnz], np.int64)
+        rec["rp_" + name] = ints[: nrow + 1]
+        rec["col_" + name] = ints[nrow + 1: nrow + 1 + nnz]
+    np.savez_compressed(os.path.join(HERE, "mtx_read.npz"), **rec)
     print("golden fixtures written to", HERE)
 
 
