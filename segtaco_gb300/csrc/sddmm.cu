@@ -6,8 +6,9 @@
 // nonzeros whose start row is the canonical block start; a group of G lanes
 // computes one dot product with V-wide loads of X[i] and Y[j] (one 16-byte load
 // per lane for D = 64 fp32 or D = 64 bf16), reduces it with xor shuffles, and
-// the 32 results of a batch leave in one coalesced store.  X[i] is re-read for
-// every nonzero of row i but stays in L1.
+// the 32 results of a batch leave in one coalesced store.  The loads of U = 4
+// steps (4P nonzeros) are issued before their multiply-adds.  X[i] is re-read
+// for every nonzero of row i but stays in L1.
 #include <climits>
 
 #include "common.cuh"
@@ -17,8 +18,8 @@ namespace segtaco {
 
 constexpr int kSddmmBlock = 256;  // nonzeros per warp
 
-template <typename XT, int V, int G>
-__global__ void __launch_bounds__(kCta) sddmm_kernel(int M, long long nnz,
+template <typename XT, int V, int G, int U = (V == 8 ? 1 : 4)>
+__global__ void __launch_bounds__(kCta, 3) sddmm_kernel(int M, long long nnz,
                                                     const int *__restrict__ row_ptr,
                                                     const int *__restrict__ col,
                                                     const float *__restrict__ val,
@@ -49,45 +50,69 @@ __global__ void __launch_bounds__(kCta) sddmm_kernel(int M, long long nnz,
     }
     const bool covered = (long long)__shfl_sync(FULL, rw, 31) > p + nb - 1;
     float res = 0.0f;
-    for (int s = 0; s * P < nb; ++s) {
-      const int t = s * P + g;
-      const int j = __shfl_sync(FULL, mc, t & 31);
-      int row = wb;
-      if (covered) {
+    const int nsteps = (nb + P - 1) / P;
+    // Steps of P nonzeros, U at a time: every load of the U steps is issued
+    // before the first multiply-add.
+    for (int s0 = 0; s0 < nsteps; s0 += U) {
+      int rows[U], js[U];
+      bool ok[U];
 #pragma unroll
-        for (int gg = 0; gg < P; ++gg) {
-          const unsigned bal = __ballot_sync(FULL, (long long)rw <= p + s * P + gg);
-          if (g == gg) row = wb + __popc(bal);
+      for (int u = 0; u < U; ++u) {
+        const int s = s0 + u;
+        const int t = s * P + g;
+        ok[u] = s < nsteps && t < nb;
+        js[u] = __shfl_sync(FULL, mc, t & 31);
+        int row = wb;
+        if (covered) {
+#pragma unroll
+          for (int gg = 0; gg < P; ++gg) {
+            const unsigned bal = __ballot_sync(FULL, (long long)rw <= p + s * P + gg);
+            if (g == gg) row = wb + __popc(bal);
+          }
+        } else if (ok[u]) {
+          int lo = wb, hi = M - 1;
+          const long long q = p + t;
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if ((long long)__ldg(row_ptr + mid) <= q)
+              lo = mid;
+            else
+              hi = mid - 1;
+          }
+          row = lo;
         }
-      } else if (t < nb) {
-        int lo = wb, hi = M - 1;
-        const long long q = p + t;
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if ((long long)__ldg(row_ptr + mid) <= q)
-            lo = mid;
-          else
-            hi = mid - 1;
-        }
-        row = lo;
+        rows[u] = row;
       }
-      float acc = 0.0f;
-      if (t < nb) {
-        const XT *xr = X + (long long)row * ldx;
-        const XT *yr = Y + (long long)j * ldy;
-        for (int k = gl * V; k < D; k += G * V) {
-          float xa[V], ya[V];
-          DenseLoad<XT, V, false>::run(xr + k, xa, 0);
-          DenseLoad<XT, V, false>::run(yr + k, ya, 0);
+      float acc[U];
 #pragma unroll
-          for (int v = 0; v < V; ++v) acc = fmaf(xa[v], ya[v], acc);
+      for (int u = 0; u < U; ++u) acc[u] = 0.0f;
+      for (int k = gl * V; k < D; k += G * V) {
+        float xa[U][V], ya[U][V];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          if (ok[u]) {
+            DenseLoad<XT, V, false>::run(X + (long long)rows[u] * ldx + k, xa[u], 0);
+            DenseLoad<XT, V, false>::run(Y + (long long)js[u] * ldy + k, ya[u], 0);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          if (ok[u]) {
+#pragma unroll
+            for (int v = 0; v < V; ++v) acc[u] = fmaf(xa[u][v], ya[u][v], acc[u]);
+          }
         }
       }
 #pragma unroll
-      for (int o = 1; o < G; o <<= 1) acc += __shfl_xor_sync(FULL, acc, o);
-      // Nonzero t of this step was reduced by group t - s*P; lane t keeps it.
-      const float r = __shfl_sync(FULL, acc, ((lane - s * P) & (P - 1)) * G);
-      if (lane / P == s) res = r;
+      for (int u = 0; u < U; ++u) {
+        float a = acc[u];
+#pragma unroll
+        for (int o = 1; o < G; o <<= 1) a += __shfl_xor_sync(FULL, a, o);
+        // Nonzero t of step s was reduced by group t - s*P; lane t keeps it.
+        const int s = s0 + u;
+        const float r = __shfl_sync(FULL, a, ((lane - s * P) & (P - 1)) * G);
+        if (lane / P == s) res = r;
+      }
     }
     if (lane < nb) out[p + lane] = mv * res;
   }

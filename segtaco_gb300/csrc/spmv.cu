@@ -4,10 +4,13 @@
 // One CTA takes one merge-path tile of kTile = 256 x 8 items (row ends +
 // nonzeros).  It stages the tile's row ends and its products a_p * x[col_p]
 // in shared memory with coalesced loads (the x gathers hit L2: x is K floats),
-// then every thread walks 8 merge items sequentially, adding finished partial
-// row sums into shared row slots.  Rows wholly inside the tile are stored once;
-// the two rows that straddle the tile edges were zeroed by the partition kernel
-// and get a reduction.
+// then every thread walks 8 merge items sequentially.  Rows that end inside a
+// thread after its first row end are stored into shared row slots directly;
+// the partials that cross thread boundaries are combined by a warp segmented
+// scan, so a row spanning the tile costs one shared atomic per warp, not one
+// per thread.  Rows wholly inside the tile are stored once to y; the two rows
+// that straddle the tile edges were zeroed by the partition kernel and get a
+// reduction.
 #include <climits>
 
 #include "common.cuh"
@@ -74,21 +77,50 @@ __global__ void __launch_bounds__(kCta) spmv_kernel(int M, const int *__restrict
   }
   int tx = lo, ty = d - lo;
   const int dend = d + kSpmvIpt < total ? d + kSpmvIpt : total;
-  float run = 0.0f;
-  bool dirty = false;
+  // A row that ends inside this thread after its first row end began here too:
+  // it is stored once.  The partial before the first row end (`first`, row
+  // r0) and the one after the last (`run`, row tx) are shared with other
+  // threads and combined by a warp segmented scan below.
+  const int r0 = tx;
+  float run = 0.0f, first = 0.0f;
+  bool ended = false;
   for (int it = d; it < dend; ++it) {
     if (s_rend[tx] <= ty) {  // row end first on ties
-      if (dirty) atomicAdd(&s_row[tx], run);
+      if (ended) {
+        s_row[tx] = run;
+      } else {
+        first = run;
+        ended = true;
+      }
       run = 0.0f;
-      dirty = false;
       ++tx;
     } else {
       run += s_prod[ty];
-      dirty = true;
       ++ty;
     }
   }
-  if (dirty) atomicAdd(&s_row[tx], run);
+  // Inclusive segmented scan over the warp's lanes of the open partials
+  // (a lane that saw a row end starts a new segment).
+  const unsigned FULL = 0xffffffffu;
+  const int lane = tid & 31;
+  float sc = run;
+  int f = ended ? 1 : 0;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const float v = __shfl_up_sync(FULL, sc, o);
+    const int fo = __shfl_up_sync(FULL, f, o);
+    if (lane >= o) {
+      if (!f) sc += v;
+      f |= fo;
+    }
+  }
+  float in = __shfl_up_sync(FULL, sc, 1);
+  if (lane == 0) in = 0.0f;
+  // The first row end of a lane closes the row open after the lanes before it
+  // (which may have begun in an earlier warp: atomic); the last lane carries
+  // the warp's open partial to the row it stops in.
+  if (ended) atomicAdd(&s_row[r0], first + in);
+  if (lane == 31 && sc != 0.0f) atomicAdd(&s_row[tx], sc);
   __syncthreads();
 
   const bool head_split = x0 < M && __ldg(row_ptr + x0) < y0;
