@@ -57,33 +57,33 @@ int launch_row_stats(const int *row_ptr, int M, unsigned long long *stats, cudaS
 // Batched merge-path partition.
 // ---------------------------------------------------------------------------
 __global__ void batch_partition_kernel(const BatchPartition *__restrict__ parts, int nparts,
-                                       long long total_edges) {
+                                       long long total_rows) {
+  // A thread per (problem, row) over every problem, M + 1 each (the last is the
+  // problem's tail), writing the chunk edges inside its row
+  // (merge_path_store_row).
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= total_edges) return;
-  int lo = 0, hi = nparts - 1;  // last part with edge_begin <= t
+  const int lane = threadIdx.x & 31;
+  const bool mine = t < total_rows;
+  int lo = 0, hi = nparts - 1;  // last part with row_begin <= t
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (parts[mid].edge_begin <= t)
+    if (parts[mid].row_begin <= t)
       lo = mid;
     else
       hi = mid - 1;
   }
   const BatchPartition &bp = parts[lo];
-  const long long c = t - bp.edge_begin;
-  long long d = c * bp.D;
-  const long long total = (long long)bp.M + bp.nnz;
-  if (d > total) d = total;
-  const int x = merge_path_x(bp.row_ptr, bp.M, bp.nnz, d);
-  const int y = (int)(d - x);
-  bp.px[c] = x;
-  bp.py[c] = y;
-  if (x < bp.M && __ldg(bp.row_ptr + x) < y) {
-    float *dst = bp.C + (long long)x * bp.ldc;
-    int k = 0;
-    if ((((uintptr_t)dst) & 15) == 0)
-      for (; k + 4 <= bp.N; k += 4) *reinterpret_cast<float4 *>(dst + k) = make_float4(0, 0, 0, 0);
-    for (; k < bp.N; ++k) dst[k] = 0.0f;
-  }
+  const long long r = t - bp.row_begin;
+  const bool small = (long long)bp.M + bp.nnz + bp.D < 0x7fffffffLL;
+  long long e_prev = 0, e_r = 0;
+  if (mine && r > 0) e_prev = (long long)__ldg(bp.row_ptr + r) + r;
+  if (mine && r < bp.M) e_r = (long long)__ldg(bp.row_ptr + r + 1) + r + 1;
+  const long long nxt = mine && r < bp.M ? ceil_div_pos(e_r, bp.D, small) : 0;
+  long long c_lo = __shfl_up_sync(0xffffffffu, nxt, 1);
+  if (lane == 0 || r == 0) c_lo = ceil_div_pos(e_prev, bp.D, small);
+  if (!mine) return;
+  merge_path_store_row(bp.row_ptr, bp.M, bp.nnz, bp.D, bp.nchunks, r, c_lo,
+                       r < bp.M ? nxt - 1 : bp.nchunks, bp.px, bp.py, bp.C, bp.ldc, bp.N);
 }
 
 // ---------------------------------------------------------------------------
@@ -206,7 +206,7 @@ void batch_layout(const segtaco_spmm_problem *probs, const SpmmPlan *plans, int 
 int batch_image(const segtaco_spmm_problem *probs, const SpmmPlan *plans, int count,
                 BatchLayout *L, char *dbase, char *img, int device) {
   std::vector<BatchPartition> parts;
-  long long edges = 0;
+  long long edges = 0, prow = 0;
   for (int i = 0; i < count; ++i) {
     if (!L->has_part[i]) continue;
     const auto &p = probs[i];
@@ -224,9 +224,12 @@ int batch_image(const segtaco_spmm_problem *probs, const SpmmPlan *plans, int co
     bp.N = p.N;
     bp.edge_begin = edges;
     edges += pl.nchunks + 1;
+    bp.row_begin = prow;
+    prow += (long long)p.M + 1;
     parts.push_back(bp);
   }
   L->total_edges = edges;
+  L->total_rows = prow;
   if (!parts.empty())
     memcpy(img + L->off_parts, parts.data(), parts.size() * sizeof(BatchPartition));
   const int sms = sm_count(device);
@@ -269,10 +272,10 @@ int batch_enqueue(const BatchLayout &L, char *dbase, cudaStream_t s, const Batch
     SEGTACO_TRY(check_cuda(cudaMemsetAsync(dbase + L.off_queues, 0,
                                            L.groups.size() * sizeof(unsigned long long), s),
                            "memset queues"));
-  if (L.total_edges > 0) {
-    const long long blocks = (L.total_edges + 255) / 256;
+  if (L.total_rows > 0) {
+    const long long blocks = (L.total_rows + 255) / 256;
     batch_partition_kernel<<<(unsigned)blocks, 256, 0, s>>>(
-        reinterpret_cast<const BatchPartition *>(dbase + L.off_parts), L.nparts, L.total_edges);
+        reinterpret_cast<const BatchPartition *>(dbase + L.off_parts), L.nparts, L.total_rows);
     SEGTACO_TRY(check_launch("batch_partition_kernel"));
   }
   for (size_t gi = 0; gi < L.groups.size(); ++gi) {

@@ -123,6 +123,7 @@ struct BatchPartition {
   long long ldc;
   int N;
   long long edge_begin;  // first global edge index of this problem
+  long long row_begin;   // first global partition thread of this problem (M + 1 each)
 };
 
 // One persistent launch of a group (host side).
@@ -154,6 +155,7 @@ struct BatchLayout {
   size_t off_parts = 0, off_queues = 0, bytes = 0;
   int nparts = 0;
   long long total_edges = 0;
+  long long total_rows = 0;  // partition threads: M + 1 per element-balanced problem
 };
 // Groups the problems by kernel variant and lays out the buffer (pure host).
 void batch_layout(const segtaco_spmm_problem *probs, const SpmmPlan *plans, int count,

@@ -247,4 +247,44 @@ __device__ __forceinline__ int merge_path_x(const int *__restrict__ row_ptr, int
   return (int)lo;
 }
 
+// Merge-path edges by rows instead of by search.  Row end r is merge item
+// e_r - 1 with e_r = row_ptr[r+1] + r + 1, so the split of diagonal d takes
+// x(d) = #{r : e_r <= d} row ends -- exactly the row merge_path_x finds.
+// Hence the chunk edges c with e_{r-1} <= c*D < e_r (e_{-1} = 0) all have
+// x = r, and one thread per row can write them; a tail thread (r = M) writes
+// the edges at or past the last row end.  Every edge is written by exactly one
+// thread, with coalesced reads of row_ptr.
+__device__ __forceinline__ long long ceil_div_pos(long long a, long long D, bool small) {
+  if (small) return (long long)(((unsigned)a + (unsigned)D - 1u) / (unsigned)D);
+  return (a + D - 1) / D;
+}
+// Stores the edges [c_lo, c_hi] of row r (0 <= r <= M), zeroing row r of C
+// (N columns) once if it straddles one of them.
+__device__ __forceinline__ void merge_path_store_row(const int *__restrict__ row_ptr, int M,
+                                                     long long nnz, long long D, long long nchunks,
+                                                     long long r, long long c_lo, long long c_hi,
+                                                     int *__restrict__ px, int *__restrict__ py,
+                                                     float *__restrict__ C, long long ldc, int N) {
+  const long long total = (long long)M + nnz;
+  if (c_hi > nchunks) c_hi = nchunks;
+  if (c_lo > c_hi) return;
+  for (long long c = c_lo; c <= c_hi; ++c) {
+    long long d = c * D;
+    if (d > total) d = total;
+    px[c] = (int)r;
+    py[c] = (int)(d - r);
+  }
+  if (C != nullptr && r < M) {
+    long long dl = c_hi * D;
+    if (dl > total) dl = total;
+    if ((long long)__ldg(row_ptr + r) < dl - r) {  // y grows with c: test the last edge
+      float *dst = C + r * ldc;
+      int k = 0;
+      if ((((uintptr_t)dst) & 15) == 0)
+        for (; k + 4 <= N; k += 4) *reinterpret_cast<float4 *>(dst + k) = make_float4(0, 0, 0, 0);
+      for (; k < N; ++k) dst[k] = 0.0f;
+    }
+  }
+}
+
 }  // namespace segtaco

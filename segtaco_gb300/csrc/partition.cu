@@ -1,8 +1,9 @@
 // partition.cu -- partition arrays over row_ptr and CSR validation.
 //
-//   merge_path_kernel        merge-path split of {row ends} U {nonzeros}; also
-//                            zeroes the C rows that straddle a chunk edge (they
-//                            are then accumulated with reductions).
+//   merge_path_kernel        merge-path split of {row ends} U {nonzeros}: a
+//                            thread per row writes the chunk edges inside it;
+//                            also zeroes the C rows that straddle a chunk edge
+//                            (they are then accumulated with reductions).
 //   block_starts_taco_kernel segTACO's block starts, taco_binarySearchBefore per
 //                            block (gpu_library.h:185-240), bit-exact.
 //   block_starts_canonical   last r with row_ptr[r] <= b*P (upper_bound - 1).
@@ -20,23 +21,21 @@ __global__ void merge_path_kernel(const int *__restrict__ row_ptr, int M, long l
                                   long long D, long long nchunks, int *__restrict__ px,
                                   int *__restrict__ py, float *__restrict__ C, long long ldc,
                                   int N) {
-  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c > nchunks) return;
-  long long d = c * D;
-  const long long total = (long long)M + nnz;
-  if (d > total) d = total;
-  const int x = merge_path_x(row_ptr, M, nnz, d);
-  const int y = (int)(d - x);
-  px[c] = x;
-  py[c] = y;
-  // Row x straddles this edge when some of its nonzeros are already behind it.
-  if (C != nullptr && x < M && __ldg(row_ptr + x) < y) {
-    float *dst = C + (long long)x * ldc;
-    int k = 0;
-    if ((((uintptr_t)dst) & 15) == 0)
-      for (; k + 4 <= N; k += 4) *reinterpret_cast<float4 *>(dst + k) = make_float4(0, 0, 0, 0);
-    for (; k < N; ++k) dst[k] = 0.0f;
-  }
+  // Thread r owns the chunk edges that fall between row end r-1 and row end r
+  // (merge_path_store_row); r = M is the tail.
+  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const bool small = (long long)M + nnz + D < 0x7fffffffLL;
+  const bool mine = r <= M;
+  long long e_prev = 0, e_r = 0;
+  if (mine && r > 0) e_prev = (long long)__ldg(row_ptr + r) + r;
+  if (r < M) e_r = (long long)__ldg(row_ptr + r + 1) + r + 1;
+  const long long nxt = r < M ? ceil_div_pos(e_r, D, small) : 0;  // first edge past row r
+  long long lo = __shfl_up_sync(0xffffffffu, nxt, 1);              // = ceil(e_{r-1} / D)
+  if (lane == 0 || r == 0) lo = ceil_div_pos(e_prev, D, small);
+  if (!mine) return;
+  merge_path_store_row(row_ptr, M, nnz, D, nchunks, r, lo, r < M ? nxt - 1 : nchunks, px, py, C,
+                       ldc, N);
 }
 
 // Same bisection as taco_binarySearchBefore (gpu_library.h:185-205).
@@ -121,8 +120,8 @@ static inline unsigned grid_for(long long n, int bs) { return (unsigned)((n + bs
 
 int launch_merge_path(const int *row_ptr, int M, long long nnz, long long D, long long nchunks,
                       int *px, int *py, float *C, long long ldc, int N, cudaStream_t s) {
-  merge_path_kernel<<<grid_for(nchunks + 1, 256), 256, 0, s>>>(row_ptr, M, nnz, D, nchunks, px, py,
-                                                               C, ldc, N);
+  merge_path_kernel<<<grid_for((long long)M + 1, 256), 256, 0, s>>>(row_ptr, M, nnz, D, nchunks,
+                                                                    px, py, C, ldc, N);
   return check_launch("merge_path_kernel");
 }
 

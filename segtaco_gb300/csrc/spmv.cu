@@ -20,6 +20,11 @@ namespace segtaco {
 
 constexpr int kSpmvIpt = 8;
 constexpr int kSpmvTile = kCta * kSpmvIpt;
+// Shared slots are skewed by one word per 32: a warp whose lanes read items 8
+// apart (the per-thread walk) then touches 32 different banks, and the
+// coalesced staging writes stay conflict-free.
+__device__ __forceinline__ int sk(int i) { return i + (i >> 5); }
+constexpr int kSpmvSlots = kSpmvTile + kSpmvTile / 32 + 2;
 
 __global__ void __launch_bounds__(kCta) spmv_kernel(int M, const int *__restrict__ row_ptr,
                                                    const int *__restrict__ col,
@@ -28,9 +33,9 @@ __global__ void __launch_bounds__(kCta) spmv_kernel(int M, const int *__restrict
                                                    float *__restrict__ y,
                                                    const int *__restrict__ px,
                                                    const int *__restrict__ py, long long ntiles) {
-  __shared__ int s_rend[kSpmvTile + 1];
-  __shared__ float s_prod[kSpmvTile];
-  __shared__ float s_row[kSpmvTile + 1];
+  __shared__ int s_rend[kSpmvSlots];
+  __shared__ float s_prod[kSpmvSlots];
+  __shared__ float s_row[kSpmvSlots];
   const long long c = blockIdx.x;
   if (c >= ntiles) return;
   const int x0 = __ldg(px + c), y0 = __ldg(py + c);
@@ -42,8 +47,8 @@ __global__ void __launch_bounds__(kCta) spmv_kernel(int M, const int *__restrict
   // Stage row ends (relative to y0) for rows x0 .. x1 (x1 only as a sentinel).
   for (int i = tid; i <= nrows; i += kCta) {
     const int r = x0 + i;
-    s_rend[i] = (r < M) ? __ldg(row_ptr + r + 1) - y0 : INT_MAX;
-    s_row[i] = 0.0f;
+    s_rend[sk(i)] = (r < M) ? __ldg(row_ptr + r + 1) - y0 : INT_MAX;
+    s_row[sk(i)] = 0.0f;
   }
   // Stage products; issue all loads of a thread before using them.
   {
@@ -58,7 +63,7 @@ __global__ void __launch_bounds__(kCta) spmv_kernel(int M, const int *__restrict
 #pragma unroll
     for (int k = 0; k < kSpmvIpt; ++k) {
       const int i = k * kCta + tid;
-      if (i < nnzs) s_prod[i] = cv[k] * __ldg(x + cj[k]);
+      if (i < nnzs) s_prod[sk(i)] = cv[k] * __ldg(x + cj[k]);
     }
   }
   __syncthreads();
@@ -70,7 +75,7 @@ __global__ void __launch_bounds__(kCta) spmv_kernel(int M, const int *__restrict
   int lo = d - nnzs < 0 ? 0 : d - nnzs, hi = d < nrows ? d : nrows;
   while (lo < hi) {
     const int pivot = (lo + hi) >> 1;
-    if (s_rend[pivot] <= d - pivot - 1)
+    if (s_rend[sk(pivot)] <= d - pivot - 1)
       lo = pivot + 1;
     else
       hi = pivot;
@@ -85,9 +90,9 @@ __global__ void __launch_bounds__(kCta) spmv_kernel(int M, const int *__restrict
   float run = 0.0f, first = 0.0f;
   bool ended = false;
   for (int it = d; it < dend; ++it) {
-    if (s_rend[tx] <= ty) {  // row end first on ties
+    if (s_rend[sk(tx)] <= ty) {  // row end first on ties
       if (ended) {
-        s_row[tx] = run;
+        s_row[sk(tx)] = run;
       } else {
         first = run;
         ended = true;
@@ -95,7 +100,7 @@ __global__ void __launch_bounds__(kCta) spmv_kernel(int M, const int *__restrict
       run = 0.0f;
       ++tx;
     } else {
-      run += s_prod[ty];
+      run += s_prod[sk(ty)];
       ++ty;
     }
   }
@@ -119,15 +124,15 @@ __global__ void __launch_bounds__(kCta) spmv_kernel(int M, const int *__restrict
   // The first row end of a lane closes the row open after the lanes before it
   // (which may have begun in an earlier warp: atomic); the last lane carries
   // the warp's open partial to the row it stops in.
-  if (ended) atomicAdd(&s_row[r0], first + in);
-  if (lane == 31 && sc != 0.0f) atomicAdd(&s_row[tx], sc);
+  if (ended) atomicAdd(&s_row[sk(r0)], first + in);
+  if (lane == 31 && sc != 0.0f) atomicAdd(&s_row[sk(tx)], sc);
   __syncthreads();
 
   const bool head_split = x0 < M && __ldg(row_ptr + x0) < y0;
   for (int i = tid; i <= nrows; i += kCta) {
     const int r = x0 + i;
     if (r >= M) break;
-    const float v = s_row[i];
+    const float v = s_row[sk(i)];
     if (i == nrows) {
       // Row x1 is unfinished: add the partial only if this tile holds some of it.
       if (y1 > y0 && __ldg(row_ptr + r) < y1) atomicAdd(y + r, v);
