@@ -104,8 +104,14 @@ class ClockSampler:
             os.close(fd)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            # nvidia-smi takes a moment to start: wait for its first sample so
+            # that sampling covers the timed region that follows
+            t0 = time.time()
+            while time.time() - t0 < 3.0 and os.path.getsize(self.path) == 0:
+                time.sleep(0.01)
+            self.first = os.path.getsize(self.path)
         except Exception:
             self.proc = None
 
@@ -117,26 +123,30 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        before, inside = [], []  # samples taken before / after the region began
         with open(self.path) as f:
-            for line in f:
-                parts = [x.strip() for x in line.split(",")]
-                if len(parts) < 9:
-                    continue
-                try:
-                    sm.append(float(parts[1]))
-                    mx.append(float(parts[2]))
-                except ValueError:
-                    continue
-                for nm, v in zip(names, parts[5:9]):
-                    if v.lower() == "active":
-                        reasons.add(nm)
+            data = f.read()
         os.unlink(self.path)
-        if not sm:
+        first = getattr(self, "first", 0)
+        pos = 0
+        for line in data.splitlines(keepends=True):
+            start, pos = pos, pos + len(line)
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rec = (float(parts[1]), float(parts[2]),
+                       {nm for nm, v in zip(names, parts[5:9]) if v.lower() == "active"})
+            except ValueError:
+                continue
+            (inside if start >= first else before).append(rec)
+        use = inside or before[-1:]  # a region shorter than the interval: the last sample
+        if not use:
             return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
-                "reasons": sorted(reasons)}
+        return {"sm_mhz": statistics.median(r[0] for r in use), "sm_max_mhz": max(r[1] for r in use),
+                "samples": len(inside), "interval_ms": 20,
+                "reasons": sorted(set().union(*(r[2] for r in use)))}
 
 
 def cpu_spmm_timed(A, B, reps, threads=0, frac=1.0):
@@ -425,6 +435,51 @@ def run_gather_ceiling(ops, stream, reps=5):
     return out
 
 
+def run_link_probe(stream, gb=1):
+    """Host<->device bandwidth over the Grace-Blackwell link: copy-engine
+    copies of pinned memory (one direction, then both at once) and the
+    SM-driven copy kernel the serving loop can use (segtaco_probe_copy)."""
+    import ctypes as C
+    import time
+    import torch
+    from segtaco_gb300 import native as N_
+    n = gb << 30
+    h = torch.empty(n, dtype=torch.uint8).pin_memory()
+    h2 = torch.empty(n, dtype=torch.uint8).pin_memory()
+    d = torch.empty(n, dtype=torch.uint8, device="cuda")
+    d2 = torch.empty(n, dtype=torch.uint8, device="cuda")
+    desc = torch.empty(256, dtype=torch.uint8, device="cuda")
+    s2 = torch.cuda.Stream()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+
+    def rate(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return round(n / ((time.perf_counter() - t) / reps) / 1e9, 1)
+
+    def both():
+        with torch.cuda.stream(stream):
+            d.copy_(h, non_blocking=True)
+        with torch.cuda.stream(s2):
+            h2.copy_(d2, non_blocking=True)
+
+    def sm(dst, src):
+        N_.check(N_.lib().segtaco_probe_copy(C.c_void_p(dst.data_ptr()), C.c_void_p(src.data_ptr()),
+                                             n, C.c_void_p(desc.data_ptr()), sms * 4, None))
+    out = {"ce_h2d_GBps": rate(lambda: d.copy_(h, non_blocking=True)),
+           "ce_d2h_GBps": rate(lambda: h.copy_(d, non_blocking=True)),
+           "ce_both_directions_GBps_each": rate(both),
+           "sm_copy_h2d_GBps": rate(lambda: sm(d, h)),
+           "sm_copy_d2h_GBps": rate(lambda: sm(h, d)),
+           "bytes_per_copy": n}
+    del h, h2, d, d2
+    return out
+
+
 def serving_stream(n_req, pool_size=1024, lam=20000.0, recent=8, p_repeat=0.8, seed=0):
     """Request stream of the serving workload: Poisson arrivals at `lam` per
     second, op SpMM or SDDMM 50/50, matrix id one of the `recent` most recently
@@ -646,9 +701,10 @@ def run_ours(args, world, rank, local):
     side = None
     if not args.no_side_ops:
         side = run_side_ops(args, N_, ops, stream, Ad, peak)
-    ceiling = None
+    ceiling = link = None
     if not args.no_probe:
         ceiling = run_gather_ceiling(ops, stream)
+        link = run_link_probe(stream)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -679,7 +735,7 @@ def run_ours(args, world, rank, local):
             "gpu_launches": args.steps * (2 if eb else 1),
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks, "schedules": schedules,
             "vendor": vendor, "batched": batched, "served": served,
-            "gather_ceiling": ceiling, "side_ops": side,
+            "gather_ceiling": ceiling, "link": link, "side_ops": side,
         }
         print(json.dumps(line), flush=True)
 
