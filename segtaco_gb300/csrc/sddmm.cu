@@ -118,6 +118,93 @@ __global__ void __launch_bounds__(kCta, 3) sddmm_kernel(int M, long long nnz,
   }
 }
 
+// Sixteen-byte vectors and D = G*V*KI: G lanes per dot product, each lane
+// KI vector loads of X[i] and of Y[j] (KI = 4 whenever D allows), so one step
+// covers P = 32/G nonzeros and its reduction takes only log2(G) shuffles.  The
+// row of every nonzero of a batch is found once (a search of the 32-row
+// window, or of row_ptr when the batch leaves it) and passed by one shuffle
+// per step.  Raw vectors stay in registers until their multiply-adds.
+template <typename XT, int V, int G, int KI>
+__global__ void __launch_bounds__(kCta, 4) sddmm_fixed_kernel(
+    int M, long long nnz, const int *__restrict__ row_ptr, const int *__restrict__ col,
+    const float *__restrict__ val, const XT *__restrict__ X, const XT *__restrict__ Y,
+    long long ldx, long long ldy, float *__restrict__ out, const int *__restrict__ starts,
+    long long nblk) {
+  constexpr int P = 32 / G;
+  using Dv = Dense<XT, V>;
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int g = lane / G, gl = lane & (G - 1);
+  const long long w = (long long)blockIdx.x * (kCta / 32) + threadIdx.x / 32;
+  if (w >= nblk) return;
+  const uint64_t pol = l2_policy_evict_normal();
+  const long long pb = w * kSddmmBlock;
+  const long long pe = pb + kSddmmBlock < nnz ? pb + kSddmmBlock : nnz;
+  int wb = __ldg(starts + w);  // row of nonzero pb
+  int rw = (wb + lane < M) ? __ldg(row_ptr + wb + 1 + lane) : INT_MAX;
+  for (long long p = pb; p < pe; p += 32) {
+    const int nb = (int)(pe - p < 32 ? pe - p : 32);
+    const int mc = lane < nb ? ld_stream(col + p + lane) : 0;
+    const float mv = lane < nb ? (val ? ld_stream(val + p + lane) : 1.0f) : 0.0f;
+    for (;;) {
+      const int adv = __popc(__ballot_sync(FULL, (long long)rw <= p));
+      if (adv == 0) break;
+      wb += adv;
+      rw = (wb + lane < M) ? __ldg(row_ptr + wb + 1 + lane) : INT_MAX;
+    }
+    // Row of nonzero p + lane.
+    const long long q = p + lane;
+    int myrow;
+    if ((long long)__shfl_sync(FULL, rw, 31) > p + nb - 1) {  // the window holds the batch
+      int rr = 0;
+#pragma unroll
+      for (int st = 16; st > 0; st >>= 1)
+        if ((long long)__shfl_sync(FULL, rw, rr + st - 1) <= q) rr += st;
+      myrow = wb + rr;
+    } else {
+      int lo = wb, hi = M - 1;
+      if (lane < nb) {
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if ((long long)__ldg(row_ptr + mid) <= q)
+            lo = mid;
+          else
+            hi = mid - 1;
+        }
+      }
+      myrow = lo;
+    }
+    float res = 0.0f;
+    const int nsteps = (nb + P - 1) / P;
+    for (int s = 0; s < nsteps; ++s) {
+      const int t = s * P + g;
+      const int j = __shfl_sync(FULL, mc, t & 31);
+      const int row = __shfl_sync(FULL, myrow, t & 31);
+      float acc = 0.0f;
+      if (t < nb) {
+        const XT *xr = X + (long long)row * ldx + gl * V;
+        const XT *yr = Y + (long long)j * ldy + gl * V;
+        typename Dv::raw_t xa[KI], ya[KI];
+#pragma unroll
+        for (int k = 0; k < KI; ++k) {
+          xa[k] = Dv::load(xr + k * G * V, pol);
+          ya[k] = Dv::load(yr + k * G * V, pol);
+        }
+#pragma unroll
+        for (int k = 0; k < KI; ++k) {
+#pragma unroll
+          for (int v = 0; v < V; ++v) acc = fmaf(Dv::get(xa[k], v), Dv::get(ya[k], v), acc);
+        }
+      }
+#pragma unroll
+      for (int o = 1; o < G; o <<= 1) acc += __shfl_xor_sync(FULL, acc, o);
+      const float r = __shfl_sync(FULL, acc, ((lane - s * P) & (P - 1)) * G);
+      if (lane / P == s) res = r;
+    }
+    if (lane < nb) out[p + lane] = mv * res;
+  }
+}
+
 #define SEGTACO_SDDMM_CASE(XT, V, G)                                                          \
   case V * 100 + G:                                                                           \
     sddmm_kernel<XT, V, G><<<grid, kCta, 0, s>>>(M, nnz, row_ptr, col, val,                   \
@@ -138,6 +225,32 @@ int launch_sddmm(int M, long long nnz, const int *row_ptr, const int *col, const
   const uintptr_t al = (uintptr_t)X | (uintptr_t)Y;
   int V = 16 / esz;
   while (V > 1 && (D % V != 0 || ldx % V != 0 || ldy % V != 0 || (al % (V * esz)) != 0)) V >>= 1;
+  // Sixteen-byte vectors with D / V a power of two up to 128: the fixed-shape
+  // kernel (KI vector loads per lane, at most 4).
+  if (V * esz == 16 && D % V == 0) {
+    const int T = D / V;
+    if (T >= 1 && T <= 128 && (T & (T - 1)) == 0) {
+      const int KI = T < 4 ? T : 4, Gf = T / KI;
+      const int key = KI * 100 + Gf;
+#define SEGTACO_SDDMM_FIXED(XT, KI_, G_)                                                    \
+  case KI_ * 100 + G_:                                                                       \
+    sddmm_fixed_kernel<XT, 16 / sizeof(XT), G_, KI_><<<grid, kCta, 0, s>>>(                  \
+        M, nnz, row_ptr, col, val, static_cast<const XT *>(X), static_cast<const XT *>(Y), ldx, \
+        ldy, out, starts, nblk);                                                             \
+    return check_launch("sddmm_fixed_kernel");
+#define SEGTACO_SDDMM_FIXED_ALL(XT)                                                          \
+  SEGTACO_SDDMM_FIXED(XT, 1, 1) SEGTACO_SDDMM_FIXED(XT, 2, 1) SEGTACO_SDDMM_FIXED(XT, 4, 1) \
+  SEGTACO_SDDMM_FIXED(XT, 4, 2) SEGTACO_SDDMM_FIXED(XT, 4, 4) SEGTACO_SDDMM_FIXED(XT, 4, 8) \
+  SEGTACO_SDDMM_FIXED(XT, 4, 16) SEGTACO_SDDMM_FIXED(XT, 4, 32)
+      if (x_dtype == SEGTACO_BF16) {
+        switch (key) { SEGTACO_SDDMM_FIXED_ALL(uint16_t) default: break; }
+      } else {
+        switch (key) { SEGTACO_SDDMM_FIXED_ALL(float) default: break; }
+      }
+#undef SEGTACO_SDDMM_FIXED_ALL
+#undef SEGTACO_SDDMM_FIXED
+    }
+  }
   // Lanes per dot product: enough to cover D in one pass, at most 32.
   int G = 1;
   while (G < 32 && G * V < D) G <<= 1;
