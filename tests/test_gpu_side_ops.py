@@ -67,6 +67,23 @@ def test_sddmm_small(cuda, name, D):
     check_vec(out.cpu().numpy(), ref, bound)
 
 
+@pytest.mark.parametrize("bf16", [False, True])
+@pytest.mark.parametrize("D", [4, 8, 16, 32, 128, 256, 512, 1024])
+def test_sddmm_fixed_shapes(cuda, D, bf16):
+    """Every shape of the fixed-shape kernel (D / vector width a power of two
+    up to 128), on a matrix with long and empty rows."""
+    A = CASES["powerlaw"]
+    X = synth.dense(A.M, D, seed=8)
+    Y = synth.dense(A.K, D, seed=9)
+    if bf16:
+        X, Y = synth.to_bf16_bits(X), synth.to_bf16_bits(Y)
+        out = ops.sddmm(dev(A), to_torch_bf16(X), to_torch_bf16(Y))
+    else:
+        out = ops.sddmm(dev(A), torch.from_numpy(X).cuda(), torch.from_numpy(Y).cuda())
+    ref, bound = O.sddmm_f64(A.row_ptr, A.col, A.val, X, Y, bf16=bf16)
+    check_vec(out.cpu().numpy(), ref, bound)
+
+
 @pytest.mark.parametrize("D", [8, 64])
 def test_sddmm_bf16(cuda, D):
     A = CASES["banded"]
