@@ -108,10 +108,7 @@ int run_spmm_planned(const SpmmPlan &plan, int M, int K, long long nnz, const in
                      float *C, long long ldc, int N, int *px, int *py, cudaStream_t s,
                      bool partition_ready = false);
 
-// ---- side ops (spmv.cu, sddmm.cu, spmspv.cu) ----
-int launch_spmv(int M, long long nnz, const int *row_ptr, const int *col, const float *val,
-                const float *x, float *y, int *px, int *py, long long D, long long nchunks,
-                cudaStream_t s);
+// ---- side ops (sddmm.cu, spmspv.cu; SpMV runs the SpMM kernel with N = 1) ----
 int launch_sddmm(int M, long long nnz, const int *row_ptr, const int *col, const float *val,
                  const void *X, const void *Y, int x_dtype, long long ldx, long long ldy, int D,
                  float *out, int *starts, int P, long long nblk, cudaStream_t s);
