@@ -17,6 +17,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "internal.h"
 #include "segtaco_taco.h"
@@ -25,6 +26,7 @@ namespace {
 
 using segtaco::set_error;
 using segtaco::check_cuda;
+using segtaco::check_launch;
 
 enum Kind { K_SPMM, K_CUSPARSE, K_SPMV, K_SDDMM, K_SPMSPV };
 
@@ -188,6 +190,198 @@ int need(const taco_tensor_t *t, const char *what, bool csr) {
   return SEGTACO_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Pipelined copies around the SpMM.  The call's time is mostly the link: the
+// operands go in and C comes out over host<->device copies.  The product is cut
+// into tiles of (column slab of B and C) x (row block of A and C):
+//   * wide N (a multiple of 32, at least 64): A goes in whole, then B one
+//     32-column slab at a time (2D copies); the tiles of slab s run as soon as
+//     slab s has landed, so C starts coming back while later slabs go in;
+//   * otherwise one slab: B and row_ptr go in first, then A's nonzeros block by
+//     block, each block's tile running once its nonzeros have landed.
+// Each tile's rows and columns of C go back (a 2D copy) while the next tiles
+// compute.  A row block is a proper CSR of its own: its row_ptr is shifted to
+// start at 0 on the device and its col / vals pointers start at its first
+// nonzero.  Row blocks are balanced by rows + nonzeros.  The timer sums the
+// tiles' compute time (segTACO times {memset, partition, kernel} only,
+// gpu_library.h:853-857).
+// ---------------------------------------------------------------------------
+__global__ void shift_rows_kernel(const int *__restrict__ src, int *__restrict__ dst, int n,
+                                  int base) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[i] - base;
+}
+
+constexpr int kMaxBlocks = 8;  // row blocks
+constexpr int kMaxSlabs = 8;   // column slabs
+constexpr int kSlabCols = 32;
+
+struct ShimStreams {
+  cudaStream_t in = nullptr, comp = nullptr, out = nullptr;
+  cudaEvent_t ready_rp = nullptr, ready_b[kMaxSlabs] = {}, ready_a[kMaxBlocks] = {};
+  cudaEvent_t done[kMaxSlabs * kMaxBlocks] = {};
+  cudaEvent_t t0[kMaxSlabs * kMaxBlocks] = {}, t1[kMaxSlabs * kMaxBlocks] = {};
+};
+
+// Streams and events of the current device, created on first use (blocking
+// streams: they also order against the legacy default stream).
+int shim_streams(ShimStreams **out) {
+  static std::mutex mu;
+  static ShimStreams per_dev[64];
+  static bool made[64] = {};
+  int dev = 0;
+  SEGTACO_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
+  if (dev < 0 || dev >= 64) return set_error(SEGTACO_EUNSUPPORTED, "device %d", dev);
+  std::lock_guard<std::mutex> lk(mu);
+  ShimStreams &S = per_dev[dev];
+  if (!made[dev]) {
+    SEGTACO_TRY(check_cuda(cudaStreamCreate(&S.in), "cudaStreamCreate"));
+    SEGTACO_TRY(check_cuda(cudaStreamCreate(&S.comp), "cudaStreamCreate"));
+    SEGTACO_TRY(check_cuda(cudaStreamCreate(&S.out), "cudaStreamCreate"));
+    auto sync_event = [](cudaEvent_t *e) {
+      return check_cuda(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate");
+    };
+    SEGTACO_TRY(sync_event(&S.ready_rp));
+    for (int i = 0; i < kMaxSlabs; ++i) SEGTACO_TRY(sync_event(&S.ready_b[i]));
+    for (int i = 0; i < kMaxBlocks; ++i) SEGTACO_TRY(sync_event(&S.ready_a[i]));
+    for (int i = 0; i < kMaxSlabs * kMaxBlocks; ++i) {
+      SEGTACO_TRY(sync_event(&S.done[i]));
+      SEGTACO_TRY(check_cuda(cudaEventCreate(&S.t0[i]), "cudaEventCreate"));
+      SEGTACO_TRY(check_cuda(cudaEventCreate(&S.t1[i]), "cudaEventCreate"));
+    }
+    made[dev] = true;
+  }
+  *out = &S;
+  return SEGTACO_OK;
+}
+
+int run_spmm_pipelined(const segtaco_config &cfg, int M, int K, long long nnz, const int *rp,
+                       const int *col, const float *val, const float *Bh, int N, float *Ch,
+                       DeviceCopies &dev) {
+  // Column slabs and row blocks (one per 32 MB of A's nonzeros and C).
+  int ns = (N >= 2 * kSlabCols && N % kSlabCols == 0) ? N / kSlabCols : 1;
+  if (ns > kMaxSlabs) ns = 1;
+  const int wcols = N / ns;
+  const double bytes = (double)nnz * 8.0 + (double)M * N * 4.0;
+  int nb = (int)(bytes / (32.0 * (1 << 20))) / ns;
+  if (nb < 1) nb = 1;
+  if (nb > kMaxBlocks) nb = kMaxBlocks;
+  if (nb > M) nb = M > 0 ? M : 1;
+  std::vector<int> rows(nb + 1, 0);
+  rows[nb] = M;
+  const long long total = (long long)M + nnz;
+  for (int b = 1; b < nb; ++b) {  // first row r with rp[r] + r >= b * total / nb
+    const long long target = total * b / nb;
+    int lo = rows[b - 1], hi = M;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if ((long long)rp[mid] + mid >= target)
+        hi = mid;
+      else
+        lo = mid + 1;
+    }
+    rows[b] = lo;
+  }
+  size_t ws = 0;
+  for (int b = 0; b < nb; ++b) {
+    size_t w = 0;
+    SEGTACO_TRY(segtaco_spmm_workspace_size(rows[b + 1] - rows[b], K, rp[rows[b + 1]] - rp[rows[b]],
+                                            wcols, SEGTACO_F32, &cfg, &w));
+    if (w > ws) ws = w;
+  }
+  void *d_rp, *d_rps, *d_col, *d_val, *d_B, *d_C, *d_ws = nullptr;
+  SEGTACO_TRY(dev.alloc(&d_rp, (size_t)(M + 1) * 4));
+  SEGTACO_TRY(dev.alloc(&d_rps, (size_t)(M + nb + 1) * 4));
+  SEGTACO_TRY(dev.alloc(&d_col, (size_t)nnz * 4));
+  SEGTACO_TRY(dev.alloc(&d_val, (size_t)nnz * 4));
+  SEGTACO_TRY(dev.alloc(&d_B, (size_t)K * N * 4));
+  SEGTACO_TRY(dev.alloc(&d_C, (size_t)M * N * 4));
+  if (ws) SEGTACO_TRY(dev.alloc(&d_ws, ws));
+  ShimStreams *S;
+  SEGTACO_TRY(shim_streams(&S));
+  auto h2d = [&](void *dst, const void *src, size_t n) {
+    return n ? check_cuda(cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, S->in), "H2D")
+             : SEGTACO_OK;
+  };
+  auto rec = [&](cudaEvent_t e, cudaStream_t st) {
+    return check_cuda(cudaEventRecord(e, st), "cudaEventRecord");
+  };
+  auto upload_block = [&](int b) {
+    const long long p0 = rp[rows[b]], p1 = rp[rows[b + 1]];
+    SEGTACO_TRY(h2d((int *)d_col + p0, col + p0, (size_t)(p1 - p0) * 4));
+    SEGTACO_TRY(h2d((float *)d_val + p0, val + p0, (size_t)(p1 - p0) * 4));
+    return rec(S->ready_a[b], S->in);
+  };
+  auto upload_slab = [&](int sl) {
+    if ((size_t)K * wcols)
+      SEGTACO_TRY(check_cuda(cudaMemcpy2DAsync((float *)d_B + sl * wcols, (size_t)N * 4,
+                                               Bh + sl * wcols, (size_t)N * 4, (size_t)wcols * 4, K,
+                                               cudaMemcpyHostToDevice, S->in),
+                             "H2D slab"));
+    return rec(S->ready_b[sl], S->in);
+  };
+  // in
+  SEGTACO_TRY(h2d(d_rp, rp, (size_t)(M + 1) * 4));
+  SEGTACO_TRY(rec(S->ready_rp, S->in));
+  if (ns == 1) {
+    SEGTACO_TRY(upload_slab(0));
+    for (int b = 0; b < nb; ++b) SEGTACO_TRY(upload_block(b));
+  } else {
+    for (int b = 0; b < nb; ++b) SEGTACO_TRY(upload_block(b));
+    for (int sl = 0; sl < ns; ++sl) SEGTACO_TRY(upload_slab(sl));
+  }
+  // compute: shifted row_ptr of every block (once row_ptr is in), then the
+  // tiles slab by slab
+  SEGTACO_TRY(check_cuda(cudaStreamWaitEvent(S->comp, S->ready_rp, 0), "cudaStreamWaitEvent"));
+  for (int b = 0; b < nb; ++b) {
+    const int r0 = rows[b], mb = rows[b + 1] - r0;
+    shift_rows_kernel<<<(mb + 1 + 255) / 256, 256, 0, S->comp>>>(
+        (const int *)d_rp + r0, (int *)d_rps + r0 + b, mb + 1, rp[r0]);
+    SEGTACO_TRY(check_launch("shift_rows_kernel"));
+  }
+  for (int sl = 0; sl < ns; ++sl) {
+    SEGTACO_TRY(check_cuda(cudaStreamWaitEvent(S->comp, S->ready_b[sl], 0), "cudaStreamWaitEvent"));
+    for (int b = 0; b < nb; ++b) {
+      const int t = sl * nb + b;
+      const int r0 = rows[b], mb = rows[b + 1] - r0;
+      const long long p0 = rp[r0], nnzb = rp[rows[b + 1]] - p0;
+      if (sl == 0 || ns == 1)
+        SEGTACO_TRY(check_cuda(cudaStreamWaitEvent(S->comp, S->ready_a[b], 0),
+                               "cudaStreamWaitEvent"));
+      SEGTACO_TRY(rec(S->t0[t], S->comp));
+      SEGTACO_TRY(segtaco_spmm(mb, K, nnzb, (const int *)d_rps + r0 + b, (const int *)d_col + p0,
+                               (const float *)d_val + p0, (const float *)d_B + sl * wcols,
+                               SEGTACO_F32, N, (float *)d_C + (long long)r0 * N + sl * wcols, N,
+                               wcols, &cfg, d_ws, ws, S->comp));
+      SEGTACO_TRY(rec(S->t1[t], S->comp));
+      SEGTACO_TRY(rec(S->done[t], S->comp));
+    }
+  }
+  // out: each tile once computed
+  for (int t = 0; t < ns * nb; ++t) {
+    const int sl = t / nb, b = t % nb;
+    const int r0 = rows[b], mb = rows[b + 1] - r0;
+    SEGTACO_TRY(check_cuda(cudaStreamWaitEvent(S->out, S->done[t], 0), "cudaStreamWaitEvent"));
+    if ((size_t)mb * wcols)
+      SEGTACO_TRY(check_cuda(cudaMemcpy2DAsync(Ch + (long long)r0 * N + sl * wcols, (size_t)N * 4,
+                                               (float *)d_C + (long long)r0 * N + sl * wcols,
+                                               (size_t)N * 4, (size_t)wcols * 4, mb,
+                                               cudaMemcpyDeviceToHost, S->out),
+                             "D2H tile"));
+  }
+  SEGTACO_TRY(check_cuda(cudaStreamSynchronize(S->out), "cudaStreamSynchronize"));
+  SEGTACO_TRY(check_cuda(cudaStreamSynchronize(S->comp), "cudaStreamSynchronize"));
+  SEGTACO_TRY(check_cuda(cudaStreamSynchronize(S->in), "cudaStreamSynchronize"));
+  float sum = 0.0f;
+  for (int t = 0; t < ns * nb; ++t) {
+    float ms = 0.0f;
+    SEGTACO_TRY(check_cuda(cudaEventElapsedTime(&ms, S->t0[t], S->t1[t]), "cudaEventElapsedTime"));
+    sum += ms;
+  }
+  g_timer_ms = sum;
+  return SEGTACO_OK;
+}
+
 int run_spmm(const Entry &e, taco_tensor_t *C, taco_tensor_t *A, taco_tensor_t *B) {
   SEGTACO_TRY(need(C, "C", false));
   SEGTACO_TRY(need(A, "A", true));
@@ -202,6 +396,15 @@ int run_spmm(const Entry &e, taco_tensor_t *C, taco_tensor_t *A, taco_tensor_t *
   if (nnz > 0 && (!col || !A->vals)) return set_error(SEGTACO_EINVAL, "A: col/vals missing");
   if (!C->vals || (!B->vals && (size_t)K * N)) return set_error(SEGTACO_EINVAL, "vals missing");
   DeviceCopies dev;
+  if (e.kind != K_CUSPARSE) {
+    segtaco_config cfg{};
+    cfg.schedule = e.schedule;
+    cfg.vec = e.vec;
+    cfg.rows_per_unit = e.rows;
+    cfg.items_per_unit = e.items;
+    cfg.col_tile = e.col_tile;
+    return run_spmm_pipelined(cfg, M, K, nnz, rp, col, A->vals, B->vals, N, C->vals, dev);
+  }
   void *d_rp, *d_col, *d_val, *d_B, *d_C;
   SEGTACO_TRY(dev.upload(&d_rp, rp, (size_t)(M + 1) * 4));
   SEGTACO_TRY(dev.upload(&d_col, col, (size_t)nnz * 4));
@@ -209,7 +412,7 @@ int run_spmm(const Entry &e, taco_tensor_t *C, taco_tensor_t *A, taco_tensor_t *
   SEGTACO_TRY(dev.upload(&d_B, B->vals, (size_t)K * N * 4));
   SEGTACO_TRY(dev.alloc(&d_C, (size_t)M * N * 4));
   RegionTimer timer;
-  if (e.kind == K_CUSPARSE) {
+  {
     cusparseHandle_t h = nullptr;
     cusparseSpMatDescr_t mA = nullptr;
     cusparseDnMatDescr_t mB = nullptr, mC = nullptr;
@@ -244,22 +447,6 @@ int run_spmm(const Entry &e, taco_tensor_t *C, taco_tensor_t *A, taco_tensor_t *
     if (h) cusparseDestroy(h);
 #undef CS
     SEGTACO_TRY(st);
-  } else {
-    segtaco_config cfg{};
-    cfg.schedule = e.schedule;
-    cfg.vec = e.vec;
-    cfg.rows_per_unit = e.rows;
-    cfg.items_per_unit = e.items;
-    cfg.col_tile = e.col_tile;
-    size_t ws = 0;
-    SEGTACO_TRY(segtaco_spmm_workspace_size(M, K, nnz, N, SEGTACO_F32, &cfg, &ws));
-    void *d_ws = nullptr;
-    if (ws) SEGTACO_TRY(dev.alloc(&d_ws, ws));
-    timer.start();
-    SEGTACO_TRY(segtaco_spmm(M, K, nnz, (const int *)d_rp, (const int *)d_col,
-                             (const float *)d_val, d_B, SEGTACO_F32, N, (float *)d_C, N, N, &cfg,
-                             d_ws, ws, nullptr));
-    SEGTACO_TRY(timer.stop());
   }
   SEGTACO_TRY(check_cuda(cudaMemcpy(C->vals, d_C, (size_t)M * N * 4, cudaMemcpyDeviceToHost),
                          "cudaMemcpy D2H"));

@@ -84,7 +84,7 @@ def call(name: str, out, a, b, c=None) -> float:
 
 def spmm(name: str, A, B: np.ndarray) -> tuple[np.ndarray, float]:
     """C = A B through the named entry point with host operands (A: synth.CSR-like)."""
-    Cm = np.zeros((A.M, B.shape[1]), np.float32)
+    Cm = np.full((A.M, B.shape[1]), np.nan, np.float32)  # every element must be written
     tA, hA = csr(A.row_ptr, A.col, A.val, A.M, A.K)
     tB, hB = dense(np.ascontiguousarray(B, np.float32))
     tC, hC = dense(Cm)

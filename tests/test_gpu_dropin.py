@@ -78,3 +78,17 @@ def test_shape_mismatch_is_an_error_not_a_fault(cuda):
     tC, h3 = taco.dense(Cm)
     with pytest.raises(N.SegtacoError):
         taco.call("spmm_eb_sr", tC, tA, tB)
+
+
+@pytest.mark.parametrize("n", [128, 96, 40])
+@pytest.mark.parametrize("name", ["spmm_eb_pr", "spmm_rb_sr"])
+def test_spmm_name_pipelined_tiles(cuda, name, n):
+    """A product large enough that the drop-in cuts it into several column
+    slabs and row blocks (copies overlapping the tiles' kernels)."""
+    A = synth.power_law(400_000, 400_000, 1.8, 20_000, 0.02, seed=31)
+    B = synth.dense(A.K, n, seed=32)
+    C, ms = taco.spmm(name, A, B)
+    assert ms > 0.0
+    ref = O.spmm_f64(A.row_ptr, A.col, A.val, B)
+    S = O.spmm_absbound(A.row_ptr, A.col, A.val, B)
+    assert O.max_bound_err(C, ref, S) <= TOL
