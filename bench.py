@@ -502,6 +502,9 @@ def serving_stream(n_req, pool_size=1024, lam=20000.0, recent=8, p_repeat=0.8, s
     return arrivals, is_spmm, ids
 
 
+_POOL_CACHE = {}  # pool matrices of a request stream, shared by the fp32 and bf16 runs
+
+
 def run_serving(args, N_, n_req=2000, bf16=False):
     """Served SpMM/SDDMM stream through segtaco_server (continuous batching over
     a device CSR cache), against the same stream in per-call mode (one request
@@ -513,7 +516,7 @@ def run_serving(args, N_, n_req=2000, bf16=False):
     from segtaco_gb300.serving import Server
 
     arrivals, is_spmm, ids = serving_stream(n_req)
-    mats = {m: synth.pool_matrix(m) for m in sorted(set(ids))}
+    mats = _POOL_CACHE.setdefault(n_req, {m: synth.pool_matrix(m) for m in sorted(set(ids))})
     maxK = max(A.K for A, _, _ in mats.values())
     maxM = max(A.M for A, _, _ in mats.values())
     bank_t = torch.from_numpy(synth.dense(max(maxK, maxM), 128, seed=5).ravel()).pin_memory()
@@ -700,6 +703,7 @@ def run_ours(args, world, rank, local):
     served = None
     if not args.no_serving:
         served = run_serving(args, N_)
+        served["bf16_operands"] = run_serving(args, N_, bf16=True)
     side = None
     if not args.no_side_ops:
         side = run_side_ops(args, N_, ops, stream, Ad, peak)
