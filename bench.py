@@ -610,6 +610,8 @@ def run_ours(args, world, rank, local):
         cfg.flags |= N_.FLAG_FLAT_WALK
     if args.depth:
         cfg.depth = args.depth
+    if args.vec:
+        cfg.vec = args.vec
     ws_bytes = max(256, ops.spmm_workspace_size(Ad, N, N_.F32, cfg))
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
 
@@ -759,6 +761,8 @@ def main():
     ap.add_argument("--l2-hints", action="store_true")
     ap.add_argument("--row-walk", action="store_true")
     ap.add_argument("--flat-walk", action="store_true")
+    ap.add_argument("--vec", type=int, default=0, choices=[0, 1, 2, 4, 8],
+                    help="dense elements per lane per step (0: the planner's)")
     ap.add_argument("--depth", type=int, default=0, choices=[0, 4, 8],
                     help="row walk: 16-byte loads in flight per lane (0: the planner's)")
     ap.add_argument("--all-schedules", action="store_true", default=True)

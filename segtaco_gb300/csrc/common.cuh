@@ -113,6 +113,22 @@ __device__ __forceinline__ float bf16hi(uint32_t w) { return __uint_as_float(w &
 // float: V in {1,2,4}; bf16 (uint16_t): V in {1,2,4,8}.
 template <typename BT, int V> struct Dense;
 
+// fp32 x 8: two sixteen-byte loads per lane, so a 32-column slab needs only
+// G = 4 lanes per nonzero and a warp has P = 8 slots.
+struct F8 {
+  float4 a, b;
+};
+template <> struct Dense<float, 8> {
+  using raw_t = F8;
+  static __device__ __forceinline__ raw_t load(const float *p, uint64_t pol) {
+    return F8{ld_b4<true>(p, pol), ld_b4<true>(p + 4, pol)};
+  }
+  static __device__ __forceinline__ float get(const raw_t &r, int v) {
+    const float4 &h = v < 4 ? r.a : r.b;
+    const int w = v & 3;
+    return w == 0 ? h.x : w == 1 ? h.y : w == 2 ? h.z : h.w;
+  }
+};
 template <> struct Dense<float, 4> {
   using raw_t = float4;
   static __device__ __forceinline__ raw_t load(const float *p, uint64_t pol) {

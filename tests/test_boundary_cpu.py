@@ -162,6 +162,11 @@ def test_workspace_and_heuristic(native_lib):
     assert L.segtaco_autotune_heuristic(10**6, 10**6, 2 * 10**7, 128, N.F32, 48679,
                                         C.byref(h)) == N.OK
     assert h.schedule == N.EB_PR
+    assert (h.col_tile, h.vec) == (32, 8)  # B beyond L2, skewed rows: 8 columns per lane
+    h.schedule = -1
+    assert L.segtaco_autotune_heuristic(262144, 262144, 19135456, 64, N.F32, 73,
+                                        C.byref(h)) == N.OK
+    assert h.schedule == N.RB_PR and h.vec == 0  # even rows: the planner's vectors
 
 
 def test_device_available_is_a_query(native_lib):

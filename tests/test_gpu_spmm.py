@@ -66,8 +66,8 @@ def test_tuning_knobs(cuda, sched):
     B = synth.dense(A.K, 64, seed=5)
     ref = spmm_ref(A, B)
     for col_tile in (4, 16, 32, 64, 128):
-        for vec, flags in ((1, 0), (2, 0), (4, 0), (4, N.FLAG_ROW_WALK), (4, N.FLAG_FLAT_WALK),
-                           (4, N.FLAG_SMEM_RING)):
+        for vec, flags in ((1, 0), (2, 0), (4, 0), (8, 0), (4, N.FLAG_ROW_WALK),
+                           (4, N.FLAG_FLAT_WALK), (4, N.FLAG_SMEM_RING)):
             for units in (1, 3, 7, 64, 1024):
                 kw = dict(schedule=sched, col_tile=col_tile, vec=vec, flags=flags)
                 if sched.startswith("rb"):
