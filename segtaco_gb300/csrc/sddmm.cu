@@ -123,7 +123,8 @@ __global__ void __launch_bounds__(kCta, 3) sddmm_kernel(int M, long long nnz,
 // covers P = 32/G nonzeros and its reduction takes only log2(G) shuffles.  The
 // row of every nonzero of a batch is found once (a search of the 32-row
 // window, or of row_ptr when the batch leaves it) and passed by one shuffle
-// per step.  Raw vectors stay in registers until their multiply-adds.
+// per step.  A group keeps its slice of X[i] in registers until its row
+// changes.  Raw vectors stay in registers until their multiply-adds.
 template <typename XT, int V, int G, int KI>
 __global__ void __launch_bounds__(kCta, 4) sddmm_fixed_kernel(
     int M, long long nnz, const int *__restrict__ row_ptr, const int *__restrict__ col,
@@ -142,6 +143,10 @@ __global__ void __launch_bounds__(kCta, 4) sddmm_fixed_kernel(
   const long long pe = pb + kSddmmBlock < nnz ? pb + kSddmmBlock : nnz;
   int wb = __ldg(starts + w);  // row of nonzero pb
   int rw = (wb + lane < M) ? __ldg(row_ptr + wb + 1 + lane) : INT_MAX;
+  // The group's slice of X[xrow] stays in registers while its nonzeros stay in
+  // that row (consecutive nonzeros of a row go to the same group's steps).
+  typename Dv::raw_t xa[KI];
+  int xrow = -1;
   for (long long p = pb; p < pe; p += 32) {
     const int nb = (int)(pe - p < 32 ? pe - p : 32);
     const int mc = lane < nb ? ld_stream(col + p + lane) : 0;
@@ -182,14 +187,16 @@ __global__ void __launch_bounds__(kCta, 4) sddmm_fixed_kernel(
       const int row = __shfl_sync(FULL, myrow, t & 31);
       float acc = 0.0f;
       if (t < nb) {
-        const XT *xr = X + (long long)row * ldx + gl * V;
-        const XT *yr = Y + (long long)j * ldy + gl * V;
-        typename Dv::raw_t xa[KI], ya[KI];
+        if (row != xrow) {  // a new row for this group: its slice of X[i]
+          const XT *xr = X + (long long)row * ldx + gl * V;
 #pragma unroll
-        for (int k = 0; k < KI; ++k) {
-          xa[k] = Dv::load(xr + k * G * V, pol);
-          ya[k] = Dv::load(yr + k * G * V, pol);
+          for (int k = 0; k < KI; ++k) xa[k] = Dv::load(xr + k * G * V, pol);
+          xrow = row;
         }
+        const XT *yr = Y + (long long)j * ldy + gl * V;
+        typename Dv::raw_t ya[KI];
+#pragma unroll
+        for (int k = 0; k < KI; ++k) ya[k] = Dv::load(yr + k * G * V, pol);
 #pragma unroll
         for (int k = 0; k < KI; ++k) {
 #pragma unroll
