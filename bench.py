@@ -505,11 +505,13 @@ def serving_stream(n_req, pool_size=1024, lam=20000.0, recent=8, p_repeat=0.8, s
 _POOL_CACHE = {}  # pool matrices of a request stream, shared by the fp32 and bf16 runs
 
 
-def run_serving(args, N_, n_req=2000, bf16=False):
+def run_serving(args, N_, n_req=2000, bf16=False, device=False):
     """Served SpMM/SDDMM stream through segtaco_server (continuous batching over
     a device CSR cache), against the same stream in per-call mode (one request
     per launch).  Dense operands come from pinned host memory and results go
-    back to pinned host memory, so every request pays its copies."""
+    back to pinned host memory, so every request pays its copies; with
+    device=True they are device-resident (SEGTACO_REQ_DEVICE_DENSE) and no
+    request crosses the link."""
     import numpy as np
     import torch
     from segtaco_gb300 import synth
@@ -522,9 +524,16 @@ def run_serving(args, N_, n_req=2000, bf16=False):
     bank_t = torch.from_numpy(synth.dense(max(maxK, maxM), 128, seed=5).ravel()).pin_memory()
     if bf16:
         bank_t = torch.from_numpy(synth.to_bf16_bits(bank_t.numpy())).pin_memory()
-    bank = bank_t.numpy()
-    arena_t = torch.empty(1 << 30, dtype=torch.float32).pin_memory()  # 4 GB of results
-    arena = arena_t.numpy()
+    if device:  # the same operands resident on the device
+        bank = bank_t.cuda()
+        if bf16:
+            bank = bank.view(torch.int16).view(torch.bfloat16)
+        arena = torch.empty(1 << 30, dtype=torch.float32, device="cuda")  # 4 GB of results
+    else:
+        bank = bank_t.numpy()
+        arena_t = torch.empty(1 << 30, dtype=torch.float32).pin_memory()  # 4 GB of results
+        arena = arena_t.numpy()
+    arena_cap = arena.numel() if device else arena.size
     keep, reqs, in_b, out_b, cursor = [], [], 0, 0, 0
     for k in range(n_req):
         A, n, _ = mats[ids[k]]
@@ -535,24 +544,26 @@ def run_serving(args, N_, n_req=2000, bf16=False):
             B = bank[:A.M * n].reshape(A.M, n)
             Y = bank[:A.K * n].reshape(A.K, n)
             size = A.nnz
-        if cursor + size > arena.size:
+        if cursor + size > arena_cap:
             cursor = 0
         out = arena[cursor:cursor + size]
         cursor += (size + 63) // 64 * 64
         if is_spmm[k]:
-            reqs.append(Server.request(N_.OP_SPMM, ids[k], B, out.reshape(A.M, n)))
-            in_b += B.nbytes
+            reqs.append(Server.request(N_.OP_SPMM, ids[k], B, out.reshape(A.M, n), device=device))
+            in_b += 0 if device else B.nbytes
         else:
-            reqs.append(Server.request(N_.OP_SDDMM, ids[k], B, out, Y=Y))
-            in_b += B.nbytes + Y.nbytes
-        out_b += size * 4
+            reqs.append(Server.request(N_.OP_SDDMM, ids[k], B, out, Y=Y, device=device))
+            in_b += 0 if device else B.nbytes + Y.nbytes
+        out_b += 0 if device else size * 4
     result = {"workload": "%d requests, Poisson arrivals at 20k/s, SpMM or SDDMM 50/50, matrix "
                           "ids from a 1024-matrix pool (%d distinct used; recent-id repeats "
-                          "p=0.8 over the last 8 ids), dense operands %s from pinned host memory"
-                          % (n_req, len(mats), "bf16" if bf16 else "fp32"),
+                          "p=0.8 over the last 8 ids), dense operands %s %s"
+                          % (n_req, len(mats), "bf16" if bf16 else "fp32",
+                             "resident on the device" if device else "from pinned host memory"),
               "h2d_bytes": in_b, "d2h_bytes": out_b}
     for mode, flags in (("batched", 0), ("per_call", N_.SERVER_PER_CALL)):
-        with Server(flags=flags, slots=1 if flags else 3) as srv:
+        with Server(flags=flags, slots=1 if flags else args.serve_slots,
+                    max_batch=args.serve_max_batch) as srv:
             for m, (A, _, _) in mats.items():
                 srv.add_matrix(m, A, pin=True)
             srv.wait(srv.replay(reqs, arrivals)[-1], -1)  # cold pass: fills the cache
@@ -560,17 +571,25 @@ def run_serving(args, N_, n_req=2000, bf16=False):
             srv.stats(reset=True)
             tickets = srv.replay(reqs, arrivals)
             srv.drain(-1)
-            st = srv.stats()
+            st = srv.stats(reset=True)
             bad = sum(1 for t in tickets if srv.wait(t, 0) != N_.OK)
+            # capacity: the same requests all arriving at once
+            burst = srv.replay(reqs, np.zeros(len(reqs)))
+            srv.drain(-1)
+            sb = srv.stats()
+            bad += sum(1 for t in burst if srv.wait(t, 0) != N_.OK)
         result[mode] = {"requests_per_s": round(st["completed"] / st["span_s"], 1),
                         "p50_us": round(st["p50_us"], 1), "p99_us": round(st["p99_us"], 1),
                         "max_us": round(st["max_us"], 1), "mean_batch": round(st["mean_batch"], 2),
                         "batches": st["batches"], "span_ms": round(st["span_s"] * 1e3, 2),
+                        "burst_requests_per_s": round(sb["completed"] / sb["span_s"], 1),
                         "failed": bad}
     result["throughput_vs_per_call"] = round(result["batched"]["requests_per_s"] /
                                              result["per_call"]["requests_per_s"], 3)
     result["p99_vs_per_call"] = round(result["per_call"]["p99_us"] /
                                       max(result["batched"]["p99_us"], 1e-9), 3)
+    result["capacity_vs_per_call"] = round(result["batched"]["burst_requests_per_s"] /
+                                           result["per_call"]["burst_requests_per_s"], 3)
     return result
 
 
@@ -706,6 +725,7 @@ def run_ours(args, world, rank, local):
     if not args.no_serving:
         served = run_serving(args, N_)
         served["bf16_operands"] = run_serving(args, N_, bf16=True)
+        served["device_operands"] = run_serving(args, N_, device=True)
     side = None
     if not args.no_side_ops:
         side = run_side_ops(args, N_, ops, stream, Ad, peak)
@@ -772,6 +792,8 @@ def main():
     ap.add_argument("--no-vendor", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serve-slots", type=int, default=4, help="serving: batches in flight")
+    ap.add_argument("--serve-max-batch", type=int, default=64, help="serving: requests per batch")
     ap.add_argument("--no-probe", action="store_true")
     ap.add_argument("--no-side-ops", action="store_true")
     args = ap.parse_args()

@@ -197,8 +197,10 @@ int segtaco_batch_destroy(segtaco_batch *batch);
                                          pointers (no staging copies)             */
 
 typedef struct segtaco_server_config {
-  int32_t max_batch;      /* requests per batch (0: 256)                          */
-  int32_t slots;          /* batches in flight, one stream each (0: 3)            */
+  int32_t max_batch;      /* requests per batch (0: 64)                           */
+  int32_t slots;          /* batches in flight, one stream each (0: 4); measured
+                             on GB300 with the served stream of the bench: 4 x 64
+                             beat 3 x 256, 6 x 32 and 8 x 16 overall             */
   int64_t cache_bytes;    /* device CSR cache cap (0: 120 GB), clamped to the
                              free HBM at creation minus reserve_bytes             */
   int64_t staging_bytes;  /* device bytes of staged dense operands in flight

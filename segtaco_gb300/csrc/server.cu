@@ -616,8 +616,8 @@ int segtaco_server_create(const segtaco_server_config *cfg, segtaco_server **out
   if (c.max_batch < 0 || c.slots < 0 || c.cache_bytes < 0 || c.staging_bytes < 0 ||
       c.reserve_bytes < 0 || c.fail_alloc_at < 0 || c.fake_delay_us < 0)
     return set_error(SEGTACO_EINVAL, "server: negative configuration value");
-  if (c.max_batch == 0) c.max_batch = 256;
-  if (c.slots == 0) c.slots = 3;
+  if (c.max_batch == 0) c.max_batch = 64;
+  if (c.slots == 0) c.slots = 4;
   if (c.slots > 16) c.slots = 16;
   if (c.cache_bytes == 0) c.cache_bytes = 120LL << 30;
   if (c.staging_bytes == 0) c.staging_bytes = 8LL << 30;
