@@ -84,7 +84,7 @@ __device__ __forceinline__ int find_problem(const long long *__restrict__ begin,
 constexpr int kBatchSmemProblems = 1024;
 
 template <typename BT, int V, int G, bool ROWS>
-__global__ void __launch_bounds__(kSpmmCta, spmm_min_ctas<V, false>())
+__global__ void __launch_bounds__(kSpmmCta, spmm_min_ctas<V, G, false>())
     spmm_batch_kernel(const BatchProblem<BT> *__restrict__ probs,
                       const long long *__restrict__ item_begin, int nprobs,
                       long long total_items, unsigned long long *__restrict__ queue,

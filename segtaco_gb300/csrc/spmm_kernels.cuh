@@ -472,16 +472,19 @@ constexpr int kWalkRows = 0, kWalkRowsDeep = 1, kWalkFlat = 2;
 
 // CTAs of the SpMM kernels: 4 warps each, so a CTA that finishes early frees
 // its slot soon (warps of a CTA walk units of uneven cost).  32 warps per SM
-// at most 64 registers; the bf16 x 8 variants and the deep row walk need more
-// registers and run 24.
+// at most 64 registers, except the variants that need more (spmm_min_ctas).
 constexpr int kSpmmCta = 128;
 constexpr int kSpmmWarps = kSpmmCta / 32;
-template <int V, bool HEAVY> constexpr int spmm_min_ctas() {
-  return ((V == 8 || HEAVY) ? 24 : 32) / kSpmmWarps;
+template <int V, int G, bool HEAVY> constexpr int spmm_min_ctas() {
+  // 8-element lanes fit 64 registers without spilling only for G <= 4 (the
+  // autotuned W = 32 case, measured by ptxas); wider groups, the flat walk
+  // with 8-element lanes and the deep row walk take 24 warps.
+  return ((HEAVY || (V == 8 && G > 4)) ? 24 : 32) / kSpmmWarps;
 }
 
 template <typename BT, int V, int G, bool ROWS, int WALK = kWalkRows>
-__global__ void __launch_bounds__(kSpmmCta, spmm_min_ctas<V, WALK == kWalkRowsDeep>())
+__global__ void __launch_bounds__(kSpmmCta, spmm_min_ctas<V, G, WALK == kWalkRowsDeep ||
+                                                                  (WALK == kWalkFlat && V == 8)>())
     spmm_seg_kernel(SpmmArgs<BT> a) {
   const long long w = (long long)blockIdx.x * kSpmmWarps + threadIdx.x / 32;
   if (w >= a.units) return;  // whole warp leaves together
