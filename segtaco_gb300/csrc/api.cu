@@ -70,13 +70,13 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
   const int esz = b_dtype == SEGTACO_BF16 ? 2 : 4;
   // Vector width: the widest 16-byte-or-less load that N, the strides and the
   // base pointers allow, for both the B loads and the C stores.
-  // fp32 also takes vec = 8 on request: two 16-byte loads per lane.
+  // fp32 also takes vec = 8 on request: one 32-byte load per lane.
   int V = c.vec > 0 ? c.vec : 16 / esz;
   if (V > 8 || !is_pow2(V))
     return set_error(SEGTACO_EINVAL, "vec=%d not in {1,2,4,8}", c.vec);
   auto fits = [&](int v) {
     const int vc = v < 4 ? v : 4;           // C is stored in float4 pieces
-    const int ab = v * esz < 16 ? v * esz : 16;  // B loads are at most 16 bytes each
+    const int ab = v * esz;                  // one B load of v elements per lane
     return N % v == 0 && ldb % v == 0 && ((uintptr_t)B % ab) == 0 && ldc % vc == 0 &&
            ((uintptr_t)C % (vc * 4)) == 0;
   };

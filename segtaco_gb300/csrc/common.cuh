@@ -120,8 +120,14 @@ struct F8 {
 };
 template <> struct Dense<float, 8> {
   using raw_t = F8;
+  // One 32-byte load (ld.global.v8.f32, sm_100+): p is 32-byte aligned.
   static __device__ __forceinline__ raw_t load(const float *p, uint64_t pol) {
-    return F8{ld_b4<true>(p, pol), ld_b4<true>(p + 4, pol)};
+    F8 r;
+    asm volatile("ld.global.nc.L2::cache_hint.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8], %9;"
+                 : "=f"(r.a.x), "=f"(r.a.y), "=f"(r.a.z), "=f"(r.a.w), "=f"(r.b.x),
+                   "=f"(r.b.y), "=f"(r.b.z), "=f"(r.b.w)
+                 : "l"(p), "l"(pol));
+    return r;
   }
   static __device__ __forceinline__ float get(const raw_t &r, int v) {
     const float4 &h = v < 4 ? r.a : r.b;

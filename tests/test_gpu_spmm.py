@@ -124,6 +124,21 @@ def test_strided_and_offset_operands(cuda, sched):
     assert torch.all(Cbig[:, :3] == 7.0)  # columns outside C untouched
 
 
+@pytest.mark.parametrize("sched", ["rb_pr", "eb_pr"])
+@pytest.mark.parametrize("offset", [4, 8])
+def test_vec8_alignment(cuda, sched, offset):
+    """8-column fp32 lanes load 32 bytes at once: a B whose base is only
+    16-byte aligned (offset 4 floats) runs with 4-column lanes, a 32-byte
+    aligned one (offset 8) with 8; both give the product."""
+    A = SMALL["powerlaw"]
+    n = 64
+    Bbig = torch.from_numpy(synth.dense(A.K, n + 16, seed=12)).cuda()
+    B = Bbig[:, offset:offset + n]  # ldb = n + 16
+    C = ops.spmm(dev(A), B, config=N.Config.make(schedule=sched, col_tile=32, vec=8))
+    torch.cuda.synchronize()
+    assert_spmm_close(C.cpu().numpy(), A, B.cpu().numpy())
+
+
 @pytest.mark.parametrize("path", list(PATHS))
 @pytest.mark.parametrize("sched", SCHEDULES)
 def test_bf16_dense_operand(cuda, sched, path):
