@@ -141,7 +141,51 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
     if (P == 1 || rend - cstart >= LONG) {
       // ---- row `cur` split over the slots --------------------------------
       zero<V>(acc);
-      for (int p = cstart; p < rend; p += 32) {
+      int p0 = cstart;
+      if constexpr (G == 1 && V * (int)sizeof(BT) <= 16) {
+        // One lane per slot: lane l takes nonzeros p+l, p+l+32, ... of blocks
+        // of 32*R directly (no shuffles), R gathers in flight, the next
+        // block's indices loading meanwhile.
+        constexpr int R = 4;
+        if (rend - p0 >= 32 * R) {
+          int jc[R];
+          float vc[R];
+#pragma unroll
+          for (int b = 0; b < R; ++b) {
+            jc[b] = ld_stream(a.col + p0 + lane + 32 * b);
+            vc[b] = ld_val(a.val, p0 + lane + 32 * b);
+          }
+          while (p0 + 32 * R <= rend) {
+            const int pn = p0 + 32 * R;
+            const bool more = pn + 32 * R <= rend;
+            int jn[R];
+            float vn[R];
+#pragma unroll
+            for (int b = 0; b < R; ++b) {
+              jn[b] = more ? ld_stream(a.col + pn + lane + 32 * b) : 0;
+              vn[b] = more ? ld_val(a.val, pn + lane + 32 * b) : 0.0f;
+            }
+            typename D::raw_t bb[R];
+#pragma unroll
+            for (int b = 0; b < R; ++b) bb[b] = D::load(Bc + (size_t)(unsigned)jc[b] * ldb, pol);
+#pragma unroll
+            for (int b = 0; b < R; ++b) {
+#pragma unroll
+              for (int v = 0; v < V; ++v) acc[v] = fmaf(vc[b], D::get(bb[b], v), acc[v]);
+            }
+#pragma unroll
+            for (int b = 0; b < R; ++b) {
+              jc[b] = jn[b];
+              vc[b] = vn[b];
+            }
+            p0 = pn;
+          }
+          // the batch buffer restarts at p0
+          mc = lane < y1 - p0 ? ld_stream(a.col + p0 + lane) : 0;
+          mv = lane < y1 - p0 ? ld_val(a.val, p0 + lane) : 0.0f;
+        }
+      }
+      for (int p = p0; p < rend; p += 32) {
         const int nb = rend - p < 32 ? rend - p : 32;
         const int nxt = p + 32 < rend ? p + 32 : rend;
         const int mcn = lane < y1 - nxt ? ld_stream(a.col + nxt + lane) : 0;

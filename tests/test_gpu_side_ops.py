@@ -39,6 +39,25 @@ def test_spmv_small(cuda, name):
     check_vec(y, O.spmv_f64(A.row_ptr, A.col, A.val, x), S)
 
 
+@pytest.mark.parametrize("name", ["powerlaw", "half_empty", "one_long_row", "empty_run"])
+def test_spmv_writes_every_row(cuda, name):
+    """y starts as NaN: every row must be written (rows split across chunks
+    are zeroed by the partition, then accumulated); values default to 1."""
+    A = CASES[name]
+    x = synth.dense(A.K, 1, seed=4).reshape(-1)
+    for with_values in (True, False):
+        Ad = dev(A, with_values=with_values)
+        y = torch.full((A.M,), float("nan"), device="cuda")
+        ops.spmv(Ad, torch.from_numpy(x).cuda(), y)
+        val = A.val if with_values else np.ones_like(A.val)
+        S = O.spmm_absbound(A.row_ptr, A.col, val, x.reshape(-1, 1)).reshape(-1)
+        check_vec(y.cpu().numpy(), O.spmv_f64(A.row_ptr, A.col, val, x), S)
+    Z = synth.random_csr(1100, 10, 0.0, seed=6)  # no nonzeros: y = 0
+    y = torch.full((Z.M,), float("nan"), device="cuda")
+    ops.spmv(dev(Z), torch.zeros(Z.K, device="cuda"), y)
+    assert torch.all(y == 0)
+
+
 def test_spmv_full_power_law(cuda):
     A = synth.power_law(seed=0)
     x = synth.dense(A.K, 1, seed=2).reshape(-1)
