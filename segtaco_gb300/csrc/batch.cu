@@ -267,7 +267,8 @@ int batch_image(const segtaco_spmm_problem *probs, const SpmmPlan *plans, int co
   return SEGTACO_OK;
 }
 
-int batch_enqueue(const BatchLayout &L, char *dbase, cudaStream_t s, const BatchGate *gate) {
+int batch_enqueue(const BatchLayout &L, char *dbase, cudaStream_t s, const BatchGate *gate,
+                  const BatchFork *fork) {
   if (!L.groups.empty())
     SEGTACO_TRY(check_cuda(cudaMemsetAsync(dbase + L.off_queues, 0,
                                            L.groups.size() * sizeof(unsigned long long), s),
@@ -278,9 +279,19 @@ int batch_enqueue(const BatchLayout &L, char *dbase, cudaStream_t s, const Batch
         reinterpret_cast<const BatchPartition *>(dbase + L.off_parts), L.nparts, L.total_rows);
     SEGTACO_TRY(check_launch("batch_partition_kernel"));
   }
+  const bool forked = fork && fork->n > 0 && !gate && L.groups.size() > 1 &&
+                      fork->join.size() >= L.groups.size();
+  if (forked) SEGTACO_TRY(check_cuda(cudaEventRecord(fork->start, s), "cudaEventRecord"));
+  std::vector<char> joined(L.groups.size(), 0);
+  int next_side = 0;
   for (size_t gi = 0; gi < L.groups.size(); ++gi) {
     const auto &g = L.groups[gi];
     if (g.total_items == 0) continue;
+    cudaStream_t gs = s;
+    if (forked && gi > 0) {
+      gs = fork->side[next_side++ % fork->n];
+      SEGTACO_TRY(check_cuda(cudaStreamWaitEvent(gs, fork->start, 0), "cudaStreamWaitEvent"));
+    }
     BatchGroupLaunch G;
     G.V = g.V;
     G.G = g.G;
@@ -292,8 +303,15 @@ int batch_enqueue(const BatchLayout &L, char *dbase, cudaStream_t s, const Batch
     G.queue = reinterpret_cast<unsigned long long *>(dbase + L.off_queues) + gi;
     G.grid = g.grid;
     G.gate = gate ? *gate : BatchGate{nullptr, 0, nullptr};
-    SEGTACO_TRY(g.dtype == SEGTACO_BF16 ? launch_batch_bf16(G, s) : launch_batch_f32(G, s));
+    SEGTACO_TRY(g.dtype == SEGTACO_BF16 ? launch_batch_bf16(G, gs) : launch_batch_f32(G, gs));
+    if (gs != s) {
+      SEGTACO_TRY(check_cuda(cudaEventRecord(fork->join[gi], gs), "cudaEventRecord"));
+      joined[gi] = 1;
+    }
   }
+  for (size_t gi = 0; gi < L.groups.size(); ++gi)
+    if (joined[gi])
+      SEGTACO_TRY(check_cuda(cudaStreamWaitEvent(s, fork->join[gi], 0), "cudaStreamWaitEvent"));
   return SEGTACO_OK;
 }
 
@@ -337,7 +355,35 @@ struct segtaco_batch {
   char *dmem = nullptr;
   cudaGraphExec_t graph = nullptr;
   int device = -1;
+  BatchFork fork;  // created on the first run with more than one group
 };
+
+namespace {
+// Side streams and events of a batch's fork (non-blocking streams, events
+// without timing), created once.
+int ensure_fork(segtaco_batch *b) {
+  const size_t ng = b->layout.groups.size();
+  if (ng < 2 || b->fork.n > 0) return SEGTACO_OK;
+  BatchFork &f = b->fork;
+  const int n = (int)std::min<size_t>(ng - 1, 4);
+  SEGTACO_TRY(check_cuda(cudaEventCreateWithFlags(&f.start, cudaEventDisableTiming), "event"));
+  f.join.assign(ng, nullptr);
+  for (size_t i = 0; i < ng; ++i)
+    SEGTACO_TRY(check_cuda(cudaEventCreateWithFlags(&f.join[i], cudaEventDisableTiming), "event"));
+  for (int i = 0; i < n; ++i)
+    SEGTACO_TRY(check_cuda(cudaStreamCreateWithFlags(&f.side[i], cudaStreamNonBlocking), "stream"));
+  f.n = n;
+  return SEGTACO_OK;
+}
+void destroy_fork(BatchFork &f) {
+  for (int i = 0; i < 4; ++i)
+    if (f.side[i]) cudaStreamDestroy(f.side[i]);
+  for (cudaEvent_t e : f.join)
+    if (e) cudaEventDestroy(e);
+  if (f.start) cudaEventDestroy(f.start);
+  f = BatchFork{};
+}
+}  // namespace
 
 extern "C" {
 
@@ -412,20 +458,22 @@ int segtaco_batch_create(int32_t count, const segtaco_spmm_problem *problems,
 
 int segtaco_batch_run(segtaco_batch *b, void *stream) {
   if (!b) return set_error(SEGTACO_EINVAL, "batch is NULL");
-  return batch_enqueue(b->layout, b->dmem, static_cast<cudaStream_t>(stream));
+  SEGTACO_TRY(ensure_fork(b));
+  return batch_enqueue(b->layout, b->dmem, static_cast<cudaStream_t>(stream), nullptr, &b->fork);
 }
 
 int segtaco_batch_run_graph(segtaco_batch *b, void *stream) {
   if (!b) return set_error(SEGTACO_EINVAL, "batch is NULL");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (!b->graph) {
+    SEGTACO_TRY(ensure_fork(b));  // side streams join the capture through events
     // Capture on a private stream so the caller's stream may be the legacy one.
     cudaStream_t cs;
     SEGTACO_TRY(check_cuda(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "stream"));
     cudaGraph_t graph = nullptr;
     int st = check_cuda(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "capture");
     if (st == SEGTACO_OK) {
-      const int est = batch_enqueue(b->layout, b->dmem, cs);
+      const int est = batch_enqueue(b->layout, b->dmem, cs, nullptr, &b->fork);
       const int cst = check_cuda(cudaStreamEndCapture(cs, &graph), "end capture");
       st = est != SEGTACO_OK ? est : cst;
     }
@@ -467,6 +515,7 @@ int segtaco_batch_info(const segtaco_batch *b, int32_t *groups, int64_t *items,
 int segtaco_batch_destroy(segtaco_batch *b) {
   if (!b) return SEGTACO_OK;
   if (b->graph) cudaGraphExecDestroy(b->graph);
+  destroy_fork(b->fork);
   if (b->dmem) cudaFree(b->dmem);
   delete b;
   return SEGTACO_OK;

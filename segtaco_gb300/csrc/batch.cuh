@@ -164,10 +164,21 @@ void batch_layout(const segtaco_spmm_problem *probs, const SpmmPlan *plans, int 
 // `img` (L->bytes, zero-filled by the caller) and sizes each group's grid.
 int batch_image(const segtaco_spmm_problem *probs, const SpmmPlan *plans, int count,
                 BatchLayout *L, char *dbase, char *img, int device);
+// Side streams over which the groups of one run are spread (optional): the
+// groups are independent persistent launches, so a later group's CTAs take the
+// SMs that an earlier group's tail leaves idle.  `join` holds one event per
+// group.
+struct BatchFork {
+  int n = 0;
+  cudaStream_t side[4] = {};
+  cudaEvent_t start = nullptr;
+  std::vector<cudaEvent_t> join;
+};
 // Enqueues one run: queue reset, merge-path partitions, one launch per group.
-// `gate` (optional) holds back problems until the host releases them.
+// `gate` (optional) holds back problems until the host releases them (its
+// runs stay on `s`).
 int batch_enqueue(const BatchLayout &L, char *dbase, cudaStream_t s,
-                  const BatchGate *gate = nullptr);
+                  const BatchGate *gate = nullptr, const BatchFork *fork = nullptr);
 
 // Shape/pointer checks of one problem (pure host).
 int check_batch_problem(const segtaco_spmm_problem &p, int index);
