@@ -56,34 +56,41 @@ int launch_row_stats(const int *row_ptr, int M, unsigned long long *stats, cudaS
 // ---------------------------------------------------------------------------
 // Batched merge-path partition.
 // ---------------------------------------------------------------------------
+constexpr int kBatchPartRows = 4;  // rows per partition thread
+
 __global__ void batch_partition_kernel(const BatchPartition *__restrict__ parts, int nparts,
                                        long long total_rows) {
-  // A thread per (problem, row) over every problem, M + 1 each (the last is the
-  // problem's tail), writing the chunk edges inside its row
-  // (merge_path_store_row).
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int lane = threadIdx.x & 31;
-  const bool mine = t < total_rows;
-  int lo = 0, hi = nparts - 1;  // last part with row_begin <= t
+  // Global rows t over every problem, M + 1 each (the last is the problem's
+  // tail); row t writes the chunk edges inside it (merge_path_store_row).  A
+  // thread walks kBatchPartRows consecutive rows, possibly across problems.
+  const long long t0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * kBatchPartRows;
+  if (t0 >= total_rows) return;
+  int lo = 0, hi = nparts - 1;  // last part with row_begin <= t0
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (parts[mid].row_begin <= t)
+    if (parts[mid].row_begin <= t0)
       lo = mid;
     else
       hi = mid - 1;
   }
-  const BatchPartition &bp = parts[lo];
-  const long long r = t - bp.row_begin;
-  const bool small = (long long)bp.M + bp.nnz + bp.D < 0x7fffffffLL;
-  long long e_prev = 0, e_r = 0;
-  if (mine && r > 0) e_prev = (long long)__ldg(bp.row_ptr + r) + r;
-  if (mine && r < bp.M) e_r = (long long)__ldg(bp.row_ptr + r + 1) + r + 1;
-  const long long nxt = mine && r < bp.M ? ceil_div_pos(e_r, bp.D, small) : 0;
-  long long c_lo = __shfl_up_sync(0xffffffffu, nxt, 1);
-  if (lane == 0 || r == 0) c_lo = ceil_div_pos(e_prev, bp.D, small);
-  if (!mine) return;
-  merge_path_store_row(bp.row_ptr, bp.M, bp.nnz, bp.D, bp.nchunks, r, c_lo,
-                       r < bp.M ? nxt - 1 : bp.nchunks, bp.px, bp.py, bp.C, bp.ldc, bp.N);
+  for (int k = 0; k < kBatchPartRows; ++k) {
+    const long long t = t0 + k;
+    if (t >= total_rows) break;
+    while (lo + 1 < nparts && parts[lo + 1].row_begin <= t) ++lo;
+    const BatchPartition &bp = parts[lo];
+    const long long r = t - bp.row_begin;
+    const bool small = (long long)bp.M + bp.nnz + bp.D < 0x7fffffffLL;
+    const long long e_prev = r > 0 ? (long long)__ldg(bp.row_ptr + r) + r : 0;
+    const long long c_lo = ceil_div_pos(e_prev, bp.D, small);
+    if (r < bp.M) {
+      const long long e_r = (long long)__ldg(bp.row_ptr + r + 1) + r + 1;
+      merge_path_store_row(bp.row_ptr, bp.M, bp.nnz, bp.D, bp.nchunks, r, c_lo,
+                           ceil_div_pos(e_r, bp.D, small) - 1, bp.px, bp.py, bp.C, bp.ldc, bp.N);
+    } else {
+      merge_path_store_row(bp.row_ptr, bp.M, bp.nnz, bp.D, bp.nchunks, r, c_lo, bp.nchunks, bp.px,
+                           bp.py, bp.C, bp.ldc, bp.N);
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -274,7 +281,8 @@ int batch_enqueue(const BatchLayout &L, char *dbase, cudaStream_t s, const Batch
                                            L.groups.size() * sizeof(unsigned long long), s),
                            "memset queues"));
   if (L.total_rows > 0) {
-    const long long blocks = (L.total_rows + 255) / 256;
+    const long long per_block = 256LL * kBatchPartRows;
+    const long long blocks = (L.total_rows + per_block - 1) / per_block;
     batch_partition_kernel<<<(unsigned)blocks, 256, 0, s>>>(
         reinterpret_cast<const BatchPartition *>(dbase + L.off_parts), L.nparts, L.total_rows);
     SEGTACO_TRY(check_launch("batch_partition_kernel"));

@@ -17,25 +17,36 @@
 
 namespace segtaco {
 
+constexpr int kPartRows = 4;  // rows per partition thread
+
 __global__ void merge_path_kernel(const int *__restrict__ row_ptr, int M, long long nnz,
                                   long long D, long long nchunks, int *__restrict__ px,
                                   int *__restrict__ py, float *__restrict__ C, long long ldc,
                                   int N) {
-  // Thread r owns the chunk edges that fall between row end r-1 and row end r
-  // (merge_path_store_row); r = M is the tail.
-  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int lane = threadIdx.x & 31;
+  // Row r owns the chunk edges that fall between row end r-1 and row end r
+  // (merge_path_store_row); r = M is the tail.  A thread walks kPartRows
+  // consecutive rows, its row_ptr loads independent of one another.
+  const long long r0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * kPartRows;
+  if (r0 > M) return;
   const bool small = (long long)M + nnz + D < 0x7fffffffLL;
-  const bool mine = r <= M;
-  long long e_prev = 0, e_r = 0;
-  if (mine && r > 0) e_prev = (long long)__ldg(row_ptr + r) + r;
-  if (r < M) e_r = (long long)__ldg(row_ptr + r + 1) + r + 1;
-  const long long nxt = r < M ? ceil_div_pos(e_r, D, small) : 0;  // first edge past row r
-  long long lo = __shfl_up_sync(0xffffffffu, nxt, 1);              // = ceil(e_{r-1} / D)
-  if (lane == 0 || r == 0) lo = ceil_div_pos(e_prev, D, small);
-  if (!mine) return;
-  merge_path_store_row(row_ptr, M, nnz, D, nchunks, r, lo, r < M ? nxt - 1 : nchunks, px, py, C,
-                       ldc, N);
+  long long e[kPartRows + 1];  // e[k] = e_{r0+k-1} = row_ptr[r0+k] + r0 + k (e_{-1} = 0)
+#pragma unroll
+  for (int k = 0; k <= kPartRows; ++k) {
+    const long long r = r0 + k;
+    e[k] = (r > 0 && r <= M) ? (long long)__ldg(row_ptr + r) + r : 0;
+  }
+  long long lo = ceil_div_pos(e[0], D, small);  // first edge at or past e_{r0-1}
+#pragma unroll
+  for (int k = 0; k < kPartRows; ++k) {
+    const long long r = r0 + k;
+    if (r < M) {
+      const long long nxt = ceil_div_pos(e[k + 1], D, small);  // first edge past row r
+      merge_path_store_row(row_ptr, M, nnz, D, nchunks, r, lo, nxt - 1, px, py, C, ldc, N);
+      lo = nxt;
+    } else if (r == M) {
+      merge_path_store_row(row_ptr, M, nnz, D, nchunks, r, lo, nchunks, px, py, C, ldc, N);
+    }
+  }
 }
 
 // Same bisection as taco_binarySearchBefore (gpu_library.h:185-205).
@@ -120,8 +131,9 @@ static inline unsigned grid_for(long long n, int bs) { return (unsigned)((n + bs
 
 int launch_merge_path(const int *row_ptr, int M, long long nnz, long long D, long long nchunks,
                       int *px, int *py, float *C, long long ldc, int N, cudaStream_t s) {
-  merge_path_kernel<<<grid_for((long long)M + 1, 256), 256, 0, s>>>(row_ptr, M, nnz, D, nchunks,
-                                                                    px, py, C, ldc, N);
+  const long long threads = ((long long)M + kPartRows) / kPartRows;  // rows 0 .. M
+  merge_path_kernel<<<grid_for(threads, 256), 256, 0, s>>>(row_ptr, M, nnz, D, nchunks, px, py, C,
+                                                           ldc, N);
   return check_launch("merge_path_kernel");
 }
 
