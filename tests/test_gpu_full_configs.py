@@ -1,0 +1,66 @@
+"""Parity at the benchmark configurations' full sizes (seeded synthetic
+stand-ins for segTACO's SuiteSparse sweep), against the FP64 oracle:
+
+* uniform 16,384 x 16,384, 16 nonzeros per row, N = 32: every schedule, every
+  element of C;
+* banded-plus-random 262,144 x 262,144 (|i - j| <= 32 plus 8 random columns
+  per row, 19,135,456 nonzeros), D = N = 64: SDDMM with fp32 and bf16 dense
+  operands (every output), and the bf16-B SpMM (every element of C).
+
+The 1M x 1M power-law SpMM and SpMV at full size are in test_gpu_spmm.py and
+test_gpu_side_ops.py; the 256-matrix pool in test_gpu_batch.py."""
+import numpy as np
+import pytest
+import torch
+
+from gpu_util import TOL, assert_spmm_close, dev, spmm_ref, to_torch_bf16
+from oracle import oracle as O
+from segtaco_gb300 import native as N
+from segtaco_gb300 import ops, synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def banded():
+    A = synth.banded_plus_random(seed=0)
+    assert A.nnz == 19_135_456
+    return A
+
+
+def test_uniform16_all_schedules(cuda):
+    A = synth.uniform_rows(seed=0)
+    assert (A.M, A.K, A.nnz) == (16384, 16384, 262_144)
+    B = synth.dense(A.K, 32, seed=1)
+    ref = spmm_ref(A, B)
+    Ad, Bd = dev(A), torch.from_numpy(B).cuda()
+    for sched in ("rb_sr", "rb_pr", "eb_sr", "eb_pr"):
+        C = torch.full((A.M, 32), float("nan"), device="cuda")
+        ops.spmm(Ad, Bd, C_out=C, config=N.Config.make(schedule=sched))
+        torch.cuda.synchronize()
+        assert_spmm_close(C.cpu().numpy(), A, B, ref=ref)
+
+
+@pytest.mark.parametrize("bf16", [False, True])
+def test_banded_sddmm_full(cuda, banded, bf16):
+    A = banded
+    X = synth.dense(A.M, 64, seed=4)
+    Y = synth.dense(A.K, 64, seed=5)
+    if bf16:
+        X, Y = synth.to_bf16_bits(X), synth.to_bf16_bits(Y)
+        Xd, Yd = to_torch_bf16(X), to_torch_bf16(Y)
+    else:
+        Xd, Yd = torch.from_numpy(X).cuda(), torch.from_numpy(Y).cuda()
+    out = torch.full((A.nnz,), float("nan"), device="cuda")
+    ops.sddmm(dev(A), Xd, Yd, out)
+    ref, bound = O.sddmm_f64(A.row_ptr, A.col, A.val, X, Y, bf16=bf16)
+    assert O.max_bound_err(out.cpu().numpy(), ref, bound) <= TOL
+
+
+def test_banded_bf16_spmm_full(cuda, banded):
+    A = banded
+    bits = synth.to_bf16_bits(synth.dense(A.K, 64, seed=6))
+    C = torch.full((A.M, 64), float("nan"), device="cuda")
+    ops.spmm(dev(A), to_torch_bf16(bits), C_out=C)
+    torch.cuda.synchronize()
+    assert_spmm_close(C.cpu().numpy(), A, bits, bf16=True)
