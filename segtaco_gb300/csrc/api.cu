@@ -249,17 +249,23 @@ int segtaco_autotune_heuristic(int32_t M, int32_t K, int64_t nnz, int32_t N, int
   // segments for the parallel schedules; the sequential ones take 16-byte
   // vectors on all 32 lanes).  A B that fits L2 whole is one slab.
   const double bbytes = (double)K * N * esz;
+  const bool skewed = mean > 0.0 && (double)max_row_len > 8.0 * mean;
   if (sequential)
     cfg->col_tile = 32 * (16 / esz);
   else
     cfg->col_tile = bbytes <= 48e6 ? (N <= 64 * 4 / esz ? N : 64 * 4 / esz) : 128 / esz;
+  // rb_sr walks its longest row in one warp per slab: with B beyond L2 and a
+  // row-length tail, 64-column fp32 slabs (two warps per long row) measured
+  // 4.37 -> 3.93 ms on the 1M x 1M power law, N = 128 (eb_sr stays at 128:
+  // 1.43 vs 1.50 ms).
+  if (schedule == SEGTACO_RB_SR && esz == 4 && bbytes > 48e6 && skewed && N > 64)
+    cfg->col_tile = 64;
   // fp32, B beyond L2 (32-column slabs) and a row-length tail (max > 8x the
-  // mean: mostly short rows): 8 columns per lane (two 16-byte loads), so a
-  // warp step covers 8 short rows instead of 4.  Measured on GB300 (1M x 1M
-  // power law, N = 128): eb_pr 1.33 -> 1.19 ms, rb_pr 2.84 -> 2.62 ms; on
-  // even rows (banded) and L2-resident B the halved occupancy loses.
-  if (!sequential && esz == 4 && bbytes > 48e6 && N % 8 == 0 && mean > 0.0 &&
-      (double)max_row_len > 8.0 * mean)
+  // mean: mostly short rows): 8 columns per lane (one 32-byte load), so a warp
+  // step covers 8 short rows instead of 4.  Measured on GB300 (1M x 1M power
+  // law, N = 128): eb_pr 1.33 -> 1.15 ms, rb_pr 2.84 -> 2.49 ms; on even rows
+  // (banded) and L2-resident B the 8-element lanes lose.
+  if (!sequential && esz == 4 && bbytes > 48e6 && N % 8 == 0 && skewed)
     cfg->vec = 8;
   cfg->items_per_unit = 512;
   cfg->rows_per_unit = schedule == SEGTACO_RB_PR || schedule == SEGTACO_RB_SR ? 4 : 1;

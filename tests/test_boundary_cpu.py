@@ -167,6 +167,11 @@ def test_workspace_and_heuristic(native_lib):
     assert L.segtaco_autotune_heuristic(262144, 262144, 19135456, 64, N.F32, 73,
                                         C.byref(h)) == N.OK
     assert h.schedule == N.RB_PR and h.vec == 0  # even rows: the planner's vectors
+    for sched, tile in ((N.RB_SR, 64), (N.EB_SR, 128)):  # sequential: 16-byte lanes, rb_sr
+        h.schedule = sched                               # halves its slab on skewed rows
+        assert L.segtaco_autotune_heuristic(10**6, 10**6, 2 * 10**7, 128, N.F32, 48679,
+                                            C.byref(h)) == N.OK
+        assert h.schedule == sched and h.col_tile == tile and h.vec == 0
 
 
 def test_device_available_is_a_query(native_lib):
