@@ -158,6 +158,28 @@ template <> struct Dense<float, 1> {
   }
   static __device__ __forceinline__ float get(const raw_t &r, int) { return r; }
 };
+// Sixteen bf16 values in one 32-byte load (ld.global.v8.b32, sm_100+): p is
+// 32-byte aligned.
+struct U8 {
+  uint4 a, b;
+};
+template <> struct Dense<uint16_t, 16> {
+  using raw_t = U8;
+  static __device__ __forceinline__ raw_t load(const uint16_t *p, uint64_t pol) {
+    U8 r;
+    asm volatile("ld.global.nc.L2::cache_hint.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8], %9;"
+                 : "=r"(r.a.x), "=r"(r.a.y), "=r"(r.a.z), "=r"(r.a.w), "=r"(r.b.x),
+                   "=r"(r.b.y), "=r"(r.b.z), "=r"(r.b.w)
+                 : "l"(p), "l"(pol));
+    return r;
+  }
+  static __device__ __forceinline__ float get(const raw_t &r, int v) {
+    const uint4 &h = v < 8 ? r.a : r.b;
+    const int q = (v & 7) >> 1;
+    const uint32_t w = q == 0 ? h.x : q == 1 ? h.y : q == 2 ? h.z : h.w;
+    return (v & 1) ? bf16hi(w) : bf16lo(w);
+  }
+};
 template <> struct Dense<uint16_t, 8> {
   using raw_t = uint4;
   static __device__ __forceinline__ raw_t load(const uint16_t *p, uint64_t pol) {

@@ -232,6 +232,49 @@ int launch_sddmm(int M, long long nnz, const int *row_ptr, const int *col, const
   const uintptr_t al = (uintptr_t)X | (uintptr_t)Y;
   int V = 16 / esz;
   while (V > 1 && (D % V != 0 || ldx % V != 0 || ldy % V != 0 || (al % (V * esz)) != 0)) V >>= 1;
+  // fp32 with D a multiple of 8 and 32-byte aligned rows: 32-byte lanes (one
+  // ld.global.v8.f32), G >= 4 lanes reading whole 128-byte lines of a row per
+  // load instruction (16-byte lanes read each line of Y in two halves, and the
+  // kernel is bound by the L1 data pipe); KI <= 2 loads per lane keep the
+  // variants within 64 registers.
+  if (esz == 4 && V == 4 && D % 8 == 0 && ldx % 8 == 0 && ldy % 8 == 0 && (al % 32) == 0) {
+    const int T = D / 8;
+    if (T >= 1 && T <= 32 && (T & (T - 1)) == 0) {
+      const int Gf = T < 4 ? T : (T / 2 > 4 ? T / 2 : 4), KI = T / Gf;
+#define SEGTACO_SDDMM_FIXED8(KI_, G_)                                                        \
+  case KI_ * 100 + G_:                                                                       \
+    sddmm_fixed_kernel<float, 8, G_, KI_><<<grid, kCta, 0, s>>>(                             \
+        M, nnz, row_ptr, col, val, static_cast<const float *>(X),                            \
+        static_cast<const float *>(Y), ldx, ldy, out, starts, nblk);                         \
+    return check_launch("sddmm_fixed_kernel");
+      switch (KI * 100 + Gf) {
+        SEGTACO_SDDMM_FIXED8(1, 1) SEGTACO_SDDMM_FIXED8(1, 2) SEGTACO_SDDMM_FIXED8(1, 4)
+        SEGTACO_SDDMM_FIXED8(2, 4) SEGTACO_SDDMM_FIXED8(2, 8) SEGTACO_SDDMM_FIXED8(2, 16)
+        default: break;
+      }
+#undef SEGTACO_SDDMM_FIXED8
+    }
+  }
+  // bf16 with D a multiple of 16 and 32-byte aligned rows: 32-byte lanes of 16
+  // values (ld.global.v8.b32), G >= 4 lanes per whole 128-byte line.
+  if (esz == 2 && V == 8 && D % 16 == 0 && ldx % 16 == 0 && ldy % 16 == 0 && (al % 32) == 0) {
+    const int T = D / 16;
+    if (T >= 1 && T <= 32 && (T & (T - 1)) == 0) {
+      const int Gf = T < 4 ? T : (T / 2 > 4 ? T / 2 : 4), KI = T / Gf;
+#define SEGTACO_SDDMM_FIXED16(KI_, G_)                                                       \
+  case KI_ * 100 + G_:                                                                       \
+    sddmm_fixed_kernel<uint16_t, 16, G_, KI_><<<grid, kCta, 0, s>>>(                         \
+        M, nnz, row_ptr, col, val, static_cast<const uint16_t *>(X),                         \
+        static_cast<const uint16_t *>(Y), ldx, ldy, out, starts, nblk);                      \
+    return check_launch("sddmm_fixed_kernel");
+      switch (KI * 100 + Gf) {
+        SEGTACO_SDDMM_FIXED16(1, 1) SEGTACO_SDDMM_FIXED16(1, 2) SEGTACO_SDDMM_FIXED16(1, 4)
+        SEGTACO_SDDMM_FIXED16(2, 4) SEGTACO_SDDMM_FIXED16(2, 8) SEGTACO_SDDMM_FIXED16(2, 16)
+        default: break;
+      }
+#undef SEGTACO_SDDMM_FIXED16
+    }
+  }
   // Sixteen-byte vectors with D / V a power of two up to 128: the fixed-shape
   // kernel (KI vector loads per lane, at most 4).
   if (V * esz == 16 && D % V == 0) {

@@ -103,6 +103,29 @@ def test_sddmm_fixed_shapes(cuda, D, bf16):
     check_vec(out.cpu().numpy(), ref, bound)
 
 
+@pytest.mark.parametrize("bf16", [False, True])
+@pytest.mark.parametrize("aligned", [True, False])
+@pytest.mark.parametrize("D", [64, 128])
+def test_sddmm_alignment(cuda, bf16, aligned, D):
+    """Rows 32-byte aligned take 32-byte lanes (8 fp32 / 16 bf16 values); a
+    base only 16-byte aligned falls back to 16-byte lanes: same results."""
+    A = CASES["powerlaw"]
+    per16 = 8 if bf16 else 4  # elements in 16 bytes
+    off = 0 if aligned else per16
+    Xh = synth.dense(A.M, D + 2 * per16, seed=10)
+    Yh = synth.dense(A.K, D + 2 * per16, seed=11)
+    if bf16:
+        Xh, Yh = synth.to_bf16_bits(Xh), synth.to_bf16_bits(Yh)
+        Xb, Yb = to_torch_bf16(Xh), to_torch_bf16(Yh)
+    else:
+        Xb, Yb = torch.from_numpy(Xh).cuda(), torch.from_numpy(Yh).cuda()
+    X, Y = Xb[:, off:off + D], Yb[:, off:off + D]  # ld = D + 32 bytes
+    out = ops.sddmm(dev(A), X, Y)
+    ref, bound = O.sddmm_f64(A.row_ptr, A.col, A.val, Xh[:, off:off + D], Yh[:, off:off + D],
+                             bf16=bf16)
+    check_vec(out.cpu().numpy(), ref, bound)
+
+
 @pytest.mark.parametrize("D", [8, 64])
 def test_sddmm_bf16(cuda, D):
     A = CASES["banded"]
