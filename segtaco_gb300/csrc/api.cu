@@ -260,12 +260,16 @@ int segtaco_autotune_heuristic(int32_t M, int32_t K, int64_t nnz, int32_t N, int
   // 1.43 vs 1.50 ms).
   if (schedule == SEGTACO_RB_SR && esz == 4 && bbytes > 48e6 && skewed && N > 64)
     cfg->col_tile = 64;
-  // fp32, B beyond L2 (32-column slabs) and a row-length tail (max > 8x the
-  // mean: mostly short rows): 8 columns per lane (one 32-byte load), so a warp
-  // step covers 8 short rows instead of 4.  Measured on GB300 (1M x 1M power
-  // law, N = 128): eb_pr 1.33 -> 1.15 ms, rb_pr 2.84 -> 2.49 ms; on even rows
-  // (banded) and L2-resident B the 8-element lanes lose.
-  if (!sequential && esz == 4 && bbytes > 48e6 && N % 8 == 0 && skewed)
+  // fp32 with B beyond L2 (32-column slabs): 8 columns per lane (one 32-byte
+  // load, 4 lanes per 128-byte segment, 8 slots), so a warp step covers 8 rows
+  // or 8 nonzeros instead of 4.  Measured on GB300: 1M x 1M power law (skewed
+  // rows), N = 128, eb_pr 1.33 -> 1.15 ms, rb_pr 2.84 -> 2.49 ms; banded
+  // 262,144 rows (even rows, 19M nonzeros), N = 64, rb_pr 0.368 -> 0.344 ms.
+  // Even rows with few nonzeros keep 4 (the 256-matrix pool, products of at
+  // most a few million nonzeros, 3.74 -> 3.87 ms with 8); with B in L2
+  // (64-column slabs: 8 lanes per slot, 24 warps per SM) the pool lost more
+  // (4.38 ms).
+  if (!sequential && esz == 4 && bbytes > 48e6 && N % 8 == 0 && (skewed || nnz >= 4000000))
     cfg->vec = 8;
   cfg->items_per_unit = 512;
   cfg->rows_per_unit = schedule == SEGTACO_RB_PR || schedule == SEGTACO_RB_SR ? 4 : 1;

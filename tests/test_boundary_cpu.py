@@ -166,7 +166,11 @@ def test_workspace_and_heuristic(native_lib):
     h.schedule = -1
     assert L.segtaco_autotune_heuristic(262144, 262144, 19135456, 64, N.F32, 73,
                                         C.byref(h)) == N.OK
-    assert h.schedule == N.RB_PR and h.vec == 0  # even rows: the planner's vectors
+    assert h.schedule == N.RB_PR and h.vec == 8  # B beyond L2: 8 columns per lane
+    h.schedule = -1
+    assert L.segtaco_autotune_heuristic(20000, 20000, 240000, 64, N.F32, 30,
+                                        C.byref(h)) == N.OK
+    assert h.vec == 0  # B in L2: the planner's 16-byte lanes
     for sched, tile in ((N.RB_SR, 64), (N.EB_SR, 128)):  # sequential: 16-byte lanes, rb_sr
         h.schedule = sched                               # halves its slab on skewed rows
         assert L.segtaco_autotune_heuristic(10**6, 10**6, 2 * 10**7, 128, N.F32, 48679,
