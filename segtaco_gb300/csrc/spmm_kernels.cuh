@@ -520,9 +520,10 @@ constexpr int kWalkRows = 0, kWalkRowsDeep = 1, kWalkFlat = 2;
 constexpr int kSpmmCta = 128;
 constexpr int kSpmmWarps = kSpmmCta / 32;
 template <int V, int G, bool HEAVY> constexpr int spmm_min_ctas() {
-  // 8-element lanes fit 64 registers without spilling only for G <= 4 (the
-  // autotuned W = 32 case, measured by ptxas); wider groups, the flat walk
-  // with 8-element lanes and the deep row walk take 24 warps.
+  // 8-element lanes fit 64 registers only for G <= 4 (the autotuned W = 32
+  // case; ptxas: fp32 V = 8, G = 4 spills 4 bytes, measured faster than 24
+  // warps without the spill); wider groups, the flat walk with 8-element
+  // lanes and the deep row walk take 24 warps.
   return ((HEAVY || (V == 8 && G > 4)) ? 24 : 32) / kSpmmWarps;
 }
 
