@@ -333,9 +333,11 @@ def _time_events(fn, stream, reps, warm=3):
     return e0.elapsed_time(e1) / reps
 
 
-def run_side_ops(args, N_, ops, stream, A_pl, peak):
+def run_side_ops(args, N_, ops, stream, A_pl, peak, A_host=None):
     """The other hot-path operations at their configurations: SpMV on the
-    power-law matrix (x of 1M fp32), SDDMM with fp32 and bf16 factors of width
+    power-law matrix (x of 1M fp32), SpMSpV on the same matrix stored by
+    columns (x with 10 % of K nonzero, distinct random indices, as segTACO's
+    spmspv_csr_gpu.h:53-72 draws them), SDDMM with fp32 and bf16 factors of width
     64 and SpMM with fp32 and bf16 B (N = 64) on the banded-plus-random matrix
     (262,144^2, ~19.1M nonzeros).  bf16 error: max over 4,096 sampled rows of
     |c - c64| / sum |a b| against an FP64 product of the same bf16 values."""
@@ -354,6 +356,24 @@ def run_side_ops(args, N_, ops, stream, A_pl, peak):
     out["spmv_power_law"] = {"ms": round(ms, 4), "GBps": round(byts / ms / 1e6, 1),
                              "roofline_frac": round(byts / ms / 1e6 / peak, 4),
                              "bytes": byts}
+    # SpMSpV, power-law matrix by columns (CSR of A^T), nx = K / 10
+    if A_host is not None:
+        At = A_host.transpose()
+        Atd = ops.DeviceCSR.from_host(At, "cuda")
+        rng = np.random.default_rng(0)
+        nx = A_host.K // 10
+        xi_h = np.sort(rng.permutation(A_host.K)[:nx]).astype(np.int32)
+        xi = torch.from_numpy(xi_h).cuda()
+        xv = torch.from_numpy(rng.uniform(-1, 1, nx).astype(np.float32)).cuda()
+        ys = torch.empty(A_host.M, dtype=torch.float32, device="cuda")
+        ms = _time_events(lambda: ops.spmspv(Atd, xi, xv, A_host.M, ys, stream=stream), stream,
+                          reps)
+        colnnz = np.diff(At.row_ptr)[xi_h].astype(np.int64)
+        byts = int(nx * 8 + (8 * nx + 8 * colnnz.sum()) + A_host.M * 4)
+        out["spmspv_power_law"] = {"ms": round(ms, 4), "GBps": round(byts / ms / 1e6, 1),
+                                   "roofline_frac": round(byts / ms / 1e6 / peak, 4),
+                                   "bytes": byts, "nx": nx}
+        del Atd
     # banded-plus-random: SDDMM and SpMM, fp32 and bf16 dense operands
     A = synth.banded_plus_random(seed=0)
     Bd = ops.DeviceCSR.from_host(A, "cuda")
@@ -404,8 +424,8 @@ def run_side_ops(args, N_, ops, stream, A_pl, peak):
             ent["max_err_vs_fp64_bf16_values"] = worst
             ent["tolerance"] = 1e-5
         out["spmm_banded_" + name] = ent
-    out["config"] = "SpMV: power-law 1Mx1M (%d nnz); banded-plus-random %dx%d, %d nnz, D=N=64" % (
-        Ad.nnz, A.M, A.K, A.nnz)
+    out["config"] = ("SpMV and SpMSpV (x 10%% nonzero): power-law 1Mx1M (%d nnz); "
+                     "banded-plus-random %dx%d, %d nnz, D=N=64" % (Ad.nnz, A.M, A.K, A.nnz))
     return out
 
 
@@ -728,7 +748,7 @@ def run_ours(args, world, rank, local):
         served["device_operands"] = run_serving(args, N_, device=True)
     side = None
     if not args.no_side_ops:
-        side = run_side_ops(args, N_, ops, stream, Ad, peak)
+        side = run_side_ops(args, N_, ops, stream, Ad, peak, A)
     ceiling = link = None
     if not args.no_probe:
         ceiling = run_gather_ceiling(ops, stream)

@@ -5,7 +5,8 @@ stand-ins for segTACO's SuiteSparse sweep), against the FP64 oracle:
   element of C;
 * banded-plus-random 262,144 x 262,144 (|i - j| <= 32 plus 8 random columns
   per row, 19,135,456 nonzeros), D = N = 64: SDDMM with fp32 and bf16 dense
-  operands (every output), and the bf16-B SpMM (every element of C).
+  operands (every output), and the bf16-B SpMM (every element of C);
+* SpMSpV on the 1M x 1M power-law matrix stored by columns, x 10 % nonzero.
 
 The 1M x 1M power-law SpMM and SpMV at full size are in test_gpu_spmm.py and
 test_gpu_side_ops.py; the 256-matrix pool in test_gpu_batch.py."""
@@ -55,6 +56,20 @@ def test_banded_sddmm_full(cuda, banded, bf16):
     ops.sddmm(dev(A), Xd, Yd, out)
     ref, bound = O.sddmm_f64(A.row_ptr, A.col, A.val, X, Y, bf16=bf16)
     assert O.max_bound_err(out.cpu().numpy(), ref, bound) <= TOL
+
+
+def test_power_law_spmspv_full(cuda):
+    """SpMSpV on the 1M x 1M power-law matrix stored by columns, x with 10 %
+    of K nonzero (distinct random indices), every element of y."""
+    A = synth.power_law(seed=0)
+    At = A.transpose()
+    rng = np.random.default_rng(0)
+    nx = A.K // 10
+    idx = np.sort(rng.permutation(A.K)[:nx]).astype(np.int32)
+    xv = rng.uniform(-1, 1, nx).astype(np.float32)
+    y = ops.spmspv(dev(At), torch.from_numpy(idx).cuda(), torch.from_numpy(xv).cuda(), A.M)
+    ref, bound = O.spmspv_f64(At.row_ptr, At.col, At.val, A.M, idx, xv)
+    assert O.max_bound_err(y.cpu().numpy(), ref, bound) <= TOL
 
 
 def test_banded_bf16_spmm_full(cuda, banded):
