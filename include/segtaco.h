@@ -159,7 +159,10 @@ typedef struct segtaco_batch segtaco_batch;
  * into the batch: later runs compute with whatever the buffers then hold. */
 int segtaco_batch_create(int32_t count, const segtaco_spmm_problem *problems,
                          const segtaco_config *configs, void *stream, segtaco_batch **out);
-/* Enqueue every product of the batch on `stream`. */
+/* Enqueue every product of the batch on `stream` (its kernel groups fork onto
+ * the batch's own side streams and join `stream` before the run ends).  Runs
+ * of one batch share its device buffers and side streams: issue them from one
+ * host thread, one after another in stream order. */
 int segtaco_batch_run(segtaco_batch *batch, void *stream);
 /* Same, through a CUDA graph captured on the first call and replayed after. */
 int segtaco_batch_run_graph(segtaco_batch *batch, void *stream);
