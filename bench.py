@@ -335,7 +335,8 @@ def _time_events(fn, stream, reps, warm=3):
 
 def run_side_ops(args, N_, ops, stream, A_pl, peak, A_host=None):
     """The other hot-path operations at their configurations: SpMV on the
-    power-law matrix (x of 1M fp32), SpMSpV on the same matrix stored by
+    power-law matrix (x of 1M fp32), the bf16-B SpMM on it (N = 128, B beyond
+    L2), SpMSpV on the same matrix stored by
     columns (x with 10 % of K nonzero, distinct random indices, as segTACO's
     spmspv_csr_gpu.h:53-72 draws them), SDDMM with fp32 and bf16 factors of width
     64 and SpMM with fp32 and bf16 B (N = 64) on the banded-plus-random matrix
@@ -356,6 +357,23 @@ def run_side_ops(args, N_, ops, stream, A_pl, peak, A_host=None):
     out["spmv_power_law"] = {"ms": round(ms, 4), "GBps": round(byts / ms / 1e6, 1),
                              "roofline_frac": round(byts / ms / 1e6 / peak, 4),
                              "bytes": byts}
+    # bf16-B SpMM on the power-law matrix (N = 128, B 256 MB: beyond L2)
+    bits = synth.to_bf16_bits(synth.dense(Ad.K, 128, seed=12))
+    Bb = torch.from_numpy(bits.view(np.int16)).cuda().view(torch.bfloat16)
+    Cb = torch.empty((Ad.M, 128), dtype=torch.float32, device="cuda")
+    cfg = N_.Config.make(schedule=N_.AUTO)
+    mx = int(A_host.row_lengths().max()) if A_host is not None else -1
+    N_.check(N_.lib().segtaco_autotune_heuristic(Ad.M, Ad.K, Ad.nnz, 128, N_.BF16, mx, cfg))
+    wsb = torch.empty(max(256, ops.spmm_workspace_size(Ad, 128, N_.BF16, cfg)), dtype=torch.uint8,
+                      device="cuda")
+    ms = _time_events(lambda: ops.spmm(Ad, Bb, C_out=Cb, config=cfg, workspace=wsb,
+                                       stream=stream), stream, reps)
+    byts = algorithmic_bytes(Ad.M, Ad.K, Ad.nnz, 128, 2)
+    out["spmm_power_law_bf16"] = {"ms": round(ms, 4), "GBps": round(byts / ms / 1e6, 1),
+                                  "roofline_frac": round(byts / ms / 1e6 / peak, 4),
+                                  "bytes": byts,
+                                  "config": {k: v for k, v in cfg.as_dict().items() if v}}
+    del Bb, Cb, wsb
     # SpMSpV, power-law matrix by columns (CSR of A^T), nx = K / 10
     if A_host is not None:
         At = A_host.transpose()

@@ -228,9 +228,10 @@ template <typename BT, int V, bool kHint> struct DenseLoad {
 
 // Store V floats (streaming: C is written once and never re-read here).
 template <int V> __device__ __forceinline__ void store_c(float *p, const float (&a)[V]) {
-  if constexpr (V == 8) {
-    __stcs(reinterpret_cast<float4 *>(p), make_float4(a[0], a[1], a[2], a[3]));
-    __stcs(reinterpret_cast<float4 *>(p) + 1, make_float4(a[4], a[5], a[6], a[7]));
+  if constexpr (V >= 8) {
+#pragma unroll
+    for (int k = 0; k < V; k += 4)
+      __stcs(reinterpret_cast<float4 *>(p + k), make_float4(a[k], a[k + 1], a[k + 2], a[k + 3]));
   } else if constexpr (V == 4) {
     __stcs(reinterpret_cast<float4 *>(p), make_float4(a[0], a[1], a[2], a[3]));
   } else if constexpr (V == 2) {
@@ -250,9 +251,9 @@ __device__ __forceinline__ void red_add2(float *p, float a, float b) {
   asm volatile("red.global.add.v2.f32 [%0], {%1,%2};" ::"l"(p), "f"(a), "f"(b) : "memory");
 }
 template <int V> __device__ __forceinline__ void atomic_add_c(float *p, const float (&a)[V]) {
-  if constexpr (V == 8) {
-    red_add4(p, a[0], a[1], a[2], a[3]);
-    red_add4(p + 4, a[4], a[5], a[6], a[7]);
+  if constexpr (V >= 8) {
+#pragma unroll
+    for (int k = 0; k < V; k += 4) red_add4(p + k, a[k], a[k + 1], a[k + 2], a[k + 3]);
   } else if constexpr (V == 4) {
     red_add4(p, a[0], a[1], a[2], a[3]);
   } else if constexpr (V == 2) {

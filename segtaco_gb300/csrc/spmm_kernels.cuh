@@ -524,7 +524,7 @@ template <int V, int G, bool HEAVY> constexpr int spmm_min_ctas() {
   // case; ptxas: fp32 V = 8, G = 4 spills 4 bytes, measured faster than 24
   // warps without the spill); wider groups, the flat walk with 8-element
   // lanes and the deep row walk take 24 warps.
-  return ((HEAVY || (V == 8 && G > 4)) ? 24 : 32) / kSpmmWarps;
+  return ((HEAVY || (V == 8 && G > 4) || V == 16) ? 24 : 32) / kSpmmWarps;
 }
 
 template <typename BT, int V, int G, bool ROWS, int WALK = kWalkRows>

@@ -47,7 +47,7 @@ inline dim3 spmm_grid(const SpmmLaunch &L) {
   X(4, 1, R) X(4, 2, R) X(4, 4, R) X(4, 8, R) X(4, 16, R) X(4, 32, R) \
   X(8, 1, R) X(8, 2, R) X(8, 4, R) X(8, 8, R) X(8, 16, R) X(8, 32, R)
 #define SEGTACO_VG_F32(X, R) SEGTACO_VG_COMMON(X, R)
-#define SEGTACO_VG_BF16(X, R) SEGTACO_VG_COMMON(X, R)
+#define SEGTACO_VG_BF16(X, R) SEGTACO_VG_COMMON(X, R) X(16, 1, R) X(16, 2, R) X(16, 4, R)
 
 // Sixteen-byte-vector variants of the other walks: the row walk with 8 loads
 // in flight per lane (kWalkRowsDeep) and the flat walk (kWalkFlat).

@@ -171,6 +171,10 @@ def test_workspace_and_heuristic(native_lib):
     assert L.segtaco_autotune_heuristic(20000, 20000, 240000, 64, N.F32, 30,
                                         C.byref(h)) == N.OK
     assert h.vec == 0  # B in L2: the planner's 16-byte lanes
+    h.schedule = -1
+    assert L.segtaco_autotune_heuristic(10**6, 10**6, 2 * 10**7, 128, N.BF16, 48679,
+                                        C.byref(h)) == N.OK
+    assert (h.col_tile, h.vec) == (64, 16)  # bf16 B beyond L2, skewed: 16 columns per lane
     for sched, tile in ((N.RB_SR, 64), (N.EB_SR, 128)):  # sequential: 16-byte lanes, rb_sr
         h.schedule = sched                               # halves its slab on skewed rows
         assert L.segtaco_autotune_heuristic(10**6, 10**6, 2 * 10**7, 128, N.F32, 48679,

@@ -81,6 +81,23 @@ def test_tuning_knobs(cuda, sched):
 
 
 @pytest.mark.parametrize("sched", SCHEDULES)
+def test_bf16_sixteen_column_lanes(cuda, sched):
+    """bf16 B with 16 columns per lane (one 32-byte load): G <= 4 groups for
+    the parallel schedules; the sequential ones and wider slabs fall back to 8;
+    a B only 16-byte aligned or a ragged N to narrower lanes."""
+    A = SMALL["powerlaw"]
+    for n, tile, off in ((64, 64, 0), (128, 64, 0), (32, 32, 0), (64, 128, 0), (64, 64, 8),
+                         (48, 64, 0)):
+        B32 = synth.dense(A.K, n + 16, seed=70 + n)
+        bits = synth.to_bf16_bits(B32)
+        Bb = to_torch_bf16(bits)[:, off:off + n]
+        C = ops.spmm(dev(A), Bb, config=N.Config.make(schedule=sched, col_tile=tile, vec=16))
+        torch.cuda.synchronize()
+        assert_spmm_close(C.cpu().numpy(), A, np.ascontiguousarray(bits[:, off:off + n]),
+                          bf16=True)
+
+
+@pytest.mark.parametrize("sched", SCHEDULES)
 def test_l2_hint_flag(cuda, sched):
     A = SMALL["uniform16"]
     B = synth.dense(A.K, 32, seed=6)
