@@ -6,7 +6,8 @@
 //   * unit  = a merge-path chunk of rows+nonzeros (element-balanced, eb_*) or a
 //             block of R consecutive rows (row-balanced, rb_*);
 //   * slab  = W = G*V dense columns (blockIdx.y), G lanes x V-wide vector loads
-//             (16 B per lane for fp32 V=4 / bf16 V=8).
+//             (16 B per lane for fp32 V=4 / bf16 V=8; 32 B, one
+//             ld.global.v8, for fp32 V=8 / bf16 V=16 when B exceeds L2).
 // The 32 lanes form P = 32/G slots of G lanes; a slot reads one W-column
 // segment of one B row per step.  The warp walks the unit's rows in order and
 // treats each row by its length (all control flow is warp-uniform):
