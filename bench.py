@@ -758,7 +758,7 @@ def run_ours(args, world, rank, local):
 
     batched = None
     if not args.no_batched:
-        batched = run_batched(args, N_, ops, stream)
+        batched = run_batched(args, N_, ops, stream, count=args.batch_count)
     served = None
     if not args.no_serving:
         served = run_serving(args, N_)
@@ -829,6 +829,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-vendor", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batch-count", type=int, default=256,
+                    help="batched: matrices of the pool (256: the benchmark's; fewer for profiling)")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serve-slots", type=int, default=4, help="serving: batches in flight")
     ap.add_argument("--serve-max-batch", type=int, default=64, help="serving: requests per batch")
