@@ -1,0 +1,65 @@
+"""Seeded random sweep over the SpMM planner's space: random shapes (empty
+rows, long rows, ragged N), fp32 and bf16 B at random offsets, and random
+combinations of schedule, slab width, lane width, unit size, depth and walk,
+each against the FP64 oracle (bound-normalised error <= 1e-5).  Combinations
+the planner rejects must fail with a status, not run."""
+import numpy as np
+import pytest
+import torch
+
+from gpu_util import assert_spmm_close, dev, to_torch_bf16
+from segtaco_gb300 import native as N
+from segtaco_gb300 import ops, synth
+
+pytestmark = pytest.mark.gpu
+CASES = 160
+
+
+def random_matrix(rng):
+    kind = rng.integers(0, 4)
+    M = int(rng.integers(1, 2500))
+    K = int(rng.integers(1, 2500))
+    seed = int(rng.integers(0, 1 << 30))
+    if kind == 0:
+        return synth.random_csr(M, K, float(rng.uniform(0, 0.02)), seed=seed,
+                                p_empty=float(rng.uniform(0, 0.6)))
+    if kind == 1:
+        rows = {int(r): int(rng.integers(1, 4 * K + 1)) for r in rng.integers(0, M, 3)}
+        return synth.random_csr(M, K, float(rng.uniform(0, 0.005)), seed=seed, long_rows=rows)
+    if kind == 2:
+        return synth.power_law(M, K, 1.8, max(1, K), 0.05, seed=seed)
+    return synth.uniform_rows(M, max(K, 16), int(rng.integers(1, 16)), seed=seed)
+
+
+@pytest.mark.parametrize("case", range(CASES))
+def test_random_config(cuda, case):
+    rng = np.random.default_rng(1000 + case)
+    A = random_matrix(rng)
+    n = int(rng.choice([1, 2, 3, 4, 7, 8, 16, 31, 32, 33, 64, 96, 128, 200]))
+    bf16 = bool(rng.integers(0, 2))
+    off = int(rng.choice([0, 1, 4, 8]))
+    B32 = synth.dense(A.K, n + 16, seed=case)
+    kw = dict(schedule=str(rng.choice(["rb_sr", "rb_pr", "eb_sr", "eb_pr"])),
+              col_tile=int(rng.choice([0, 4, 8, 16, 32, 64, 128, 256])),
+              vec=int(rng.choice([0, 1, 2, 4, 8] + ([16] if bf16 else []))),
+              items_per_unit=int(rng.choice([0, 1, 7, 64, 512, 4096])),
+              rows_per_unit=int(rng.choice([0, 1, 3, 8])),
+              depth=int(rng.choice([0, 4, 8])),
+              flags=int(rng.choice([0, N.FLAG_ROW_WALK, N.FLAG_FLAT_WALK, N.FLAG_L2_HINTS])))
+    cfg = N.Config.make(**kw)
+    if bf16:
+        bits = synth.to_bf16_bits(B32)
+        Bd = to_torch_bf16(bits)[:, off:off + n]
+        Bref = np.ascontiguousarray(bits[:, off:off + n])
+    else:
+        Bd = torch.from_numpy(B32).cuda()[:, off:off + n]
+        Bref = np.ascontiguousarray(B32[:, off:off + n])
+    C = torch.full((A.M, n), float("nan"), device="cuda")
+    try:
+        ops.spmm(dev(A), Bd, C_out=C, config=cfg)
+    except N.SegtacoError as e:
+        # the planner's refusals: a status, never a launch
+        assert e.code in (N.EINVAL, N.EUNSUPPORTED), (kw, e)
+        return
+    torch.cuda.synchronize()
+    assert_spmm_close(C.cpu().numpy(), A, Bref, bf16=bf16)
