@@ -2,12 +2,14 @@
 rows, long rows, ragged N), fp32 and bf16 B at random offsets, and random
 combinations of schedule, slab width, lane width, unit size, depth and walk,
 each against the FP64 oracle (bound-normalised error <= 1e-5).  Combinations
-the planner rejects must fail with a status, not run."""
+the planner rejects must fail with a status, not run.  The same random shapes
+drive SDDMM (random D, fp32 / bf16 factors at offsets) and SpMV / SpMSpV."""
 import numpy as np
 import pytest
 import torch
 
-from gpu_util import assert_spmm_close, dev, to_torch_bf16
+from gpu_util import TOL, assert_spmm_close, dev, to_torch_bf16
+from oracle import oracle as O
 from segtaco_gb300 import native as N
 from segtaco_gb300 import ops, synth
 
@@ -63,3 +65,44 @@ def test_random_config(cuda, case):
         return
     torch.cuda.synchronize()
     assert_spmm_close(C.cpu().numpy(), A, Bref, bf16=bf16)
+
+
+@pytest.mark.parametrize("case", range(60))
+def test_random_sddmm(cuda, case):
+    rng = np.random.default_rng(5000 + case)
+    A = random_matrix(rng)
+    D = int(rng.choice([1, 3, 4, 8, 16, 24, 32, 64, 96, 128, 256, 300]))
+    bf16 = bool(rng.integers(0, 2))
+    off = int(rng.choice([0, 1, 4, 8, 16]))
+    X = synth.dense(A.M, D + 32, seed=case)
+    Y = synth.dense(A.K, D + 32, seed=case + 1)
+    if bf16:
+        X, Y = synth.to_bf16_bits(X), synth.to_bf16_bits(Y)
+        Xd, Yd = to_torch_bf16(X)[:, off:off + D], to_torch_bf16(Y)[:, off:off + D]
+    else:
+        Xd = torch.from_numpy(X).cuda()[:, off:off + D]
+        Yd = torch.from_numpy(Y).cuda()[:, off:off + D]
+    out = torch.full((A.nnz,), float("nan"), device="cuda")
+    ops.sddmm(dev(A), Xd, Yd, out)
+    ref, bound = O.sddmm_f64(A.row_ptr, A.col, A.val, np.ascontiguousarray(X[:, off:off + D]),
+                             np.ascontiguousarray(Y[:, off:off + D]), bf16=bf16)
+    if ref.size:
+        assert O.max_bound_err(out.cpu().numpy(), ref, bound) <= TOL
+
+
+@pytest.mark.parametrize("case", range(40))
+def test_random_spmv_spmspv(cuda, case):
+    rng = np.random.default_rng(7000 + case)
+    A = random_matrix(rng)
+    x = synth.dense(A.K, 1, seed=case).reshape(-1)
+    y = torch.full((A.M,), float("nan"), device="cuda")
+    ops.spmv(dev(A), torch.from_numpy(x).cuda(), y)
+    S = O.spmm_absbound(A.row_ptr, A.col, A.val, x.reshape(-1, 1)).reshape(-1)
+    assert O.max_bound_err(y.cpu().numpy(), O.spmv_f64(A.row_ptr, A.col, A.val, x), S) <= TOL
+    At = A.transpose()
+    nx = int(rng.integers(0, A.K + 1))
+    idx = np.sort(rng.permutation(A.K)[:nx]).astype(np.int32)
+    xv = rng.uniform(-1, 1, nx).astype(np.float32)
+    ys = ops.spmspv(dev(At), torch.from_numpy(idx).cuda(), torch.from_numpy(xv).cuda(), A.M)
+    ref, bound = O.spmspv_f64(At.row_ptr, At.col, At.val, A.M, idx, xv)
+    assert O.max_bound_err(ys.cpu().numpy(), ref, bound) <= TOL
