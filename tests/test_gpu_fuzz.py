@@ -106,3 +106,44 @@ def test_random_spmv_spmspv(cuda, case):
     ys = ops.spmspv(dev(At), torch.from_numpy(idx).cuda(), torch.from_numpy(xv).cuda(), A.M)
     ref, bound = O.spmspv_f64(At.row_ptr, At.col, At.val, A.M, idx, xv)
     assert O.max_bound_err(ys.cpu().numpy(), ref, bound) <= TOL
+
+
+@pytest.mark.parametrize("case", range(20))
+def test_random_batch(cuda, case):
+    """A batch of 3-16 random problems, each with its own random config and
+    dtype (so several kernel-variant groups), run directly and through the
+    captured graph."""
+    rng = np.random.default_rng(9000 + case)
+    items, refs, cfgs = [], [], []
+    for m in range(int(rng.integers(3, 17))):
+        A = random_matrix(rng)
+        n = int(rng.choice([1, 4, 8, 16, 33, 64, 128]))
+        bf16 = bool(rng.integers(0, 2))
+        B32 = synth.dense(A.K, n, seed=100 * case + m)
+        if bf16:
+            bits = synth.to_bf16_bits(B32)
+            Bd, Bref = to_torch_bf16(bits), bits
+        else:
+            Bd, Bref = torch.from_numpy(B32).cuda(), B32
+        Cd = torch.full((A.M, n), float("nan"), device="cuda")
+        items.append((dev(A), Bd, Cd))
+        refs.append((A, Bref, bf16))
+        cfgs.append(N.Config.make(
+            schedule=str(rng.choice(["rb_sr", "rb_pr", "eb_sr", "eb_pr"])),
+            col_tile=int(rng.choice([0, 16, 32, 64, 128])),
+            vec=int(rng.choice([0, 1, 2, 4, 8] + ([16] if bf16 else []))),
+            items_per_unit=int(rng.choice([0, 7, 64, 512])),
+            rows_per_unit=int(rng.choice([0, 1, 3, 8]))))
+    try:
+        b = ops.Batch(items, configs=cfgs)
+    except N.SegtacoError as e:
+        assert e.code in (N.EINVAL, N.EUNSUPPORTED), e
+        return
+    for graph in (False, True, True):
+        for _, _, Cd in items:
+            Cd.fill_(float("nan"))
+        b.run(graph=graph)
+        torch.cuda.synchronize()
+        for (_, _, Cd), (A, Bref, bf16) in zip(items, refs):
+            assert_spmm_close(Cd.cpu().numpy(), A, Bref, bf16=bf16)
+    b.close()
