@@ -73,10 +73,10 @@ extern "C" {
 typedef struct segtaco_config {
   int32_t schedule;       /* SEGTACO_RB_SR .. SEGTACO_EB_PR, or SEGTACO_AUTO    */
   int32_t col_tile;       /* W: dense columns per CTA column slab (multiple of vec) */
-  int32_t vec;            /* dense elements per lane per load: 1, 2, 4 or 8 (8 fp32
-                             or 16 bf16 = one 32-byte load, B 32-byte aligned;
-                             the planner narrows it to what N, ldb and the
-                             pointers allow)                                   */
+  int32_t vec;            /* dense elements per lane per load: 1, 2, 4, 8 (bf16
+                             also 16); 8 fp32 / 16 bf16 is one 32-byte load (B
+                             32-byte aligned).  The planner narrows it to what
+                             N, ldb and the pointers allow                     */
   int32_t rows_per_unit;  /* rb: rows handled by one lane group / warp            */
   int32_t items_per_unit; /* eb: merge-path items (rows + nonzeros) per unit      */
   uint32_t flags;         /* SEGTACO_FLAG_*                                        */
