@@ -797,7 +797,12 @@ def run_ours(args, world, rank, local):
                          "traffic": traffic, "kernel": kernel_name,
                          "gathered_bytes": A.nnz * N * 4,
                          "gather_GBps": round(A.nnz * N * 4 / kern_ms / 1e6, 1),
-                         "kernel_ms": round(kern_ms, 4), "peak_source": peak_kind + " hbm_gbs"},
+                         "kernel_ms": round(kern_ms, 4), "peak_source": peak_kind + " hbm_gbs",
+                         # the DRAM bytes ncu measured per launch over the live kernel time:
+                         # how close the kernel runs to HBM for the traffic it causes
+                         "traffic_GBps": (round(traffic / kern_ms / 1e6, 1) if traffic else None),
+                         "traffic_frac": (round(traffic / kern_ms / 1e6 / peak, 4)
+                                          if traffic else None)},
             "gpu_launches": args.steps * (2 if eb else 1),
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks, "schedules": schedules,
             "vendor": vendor, "batched": batched, "served": served,
