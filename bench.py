@@ -86,8 +86,58 @@ def committed_traffic(workload, kernel):
         return None
 
 
+class NvmlReader:
+    """Read-only NVML queries (the driver's libnvidia-ml) of the SM clock, its
+    maximum and the clock-event reasons, polled by a thread every ~1 ms so a
+    region of a few tens of milliseconds still gets many samples.  Settings are
+    never changed.  Unavailable NVML leaves it empty."""
+    BITS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+            0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, index):
+        import ctypes as C
+        import threading
+        self.samples, self._stop, self._t = [], threading.Event(), None
+        try:
+            lib = C.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return
+            h = C.c_void_p()
+            if lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(index), C.byref(h)) != 0:
+                return
+            reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                lib.nvmlDeviceGetCurrentClocksThrottleReasons
+            self._q = (lib, h, reasons, C)
+        except Exception:
+            self._q = None
+
+    def _poll(self):
+        lib, h, reasons, C = self._q
+        clk, mx, rs = C.c_uint(), C.c_uint(), C.c_ulonglong()
+        while not self._stop.is_set():
+            if (lib.nvmlDeviceGetClockInfo(h, 1, C.byref(clk)) == 0 and
+                    lib.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx)) == 0 and
+                    reasons(h, C.byref(rs)) == 0):
+                self.samples.append((float(clk.value), float(mx.value),
+                                     {n for b, n in self.BITS.items() if rs.value & b}))
+            time.sleep(0.001)
+
+    def start(self):
+        import threading
+        if getattr(self, "_q", None):
+            self._t = threading.Thread(target=self._poll, daemon=True)
+            self._t.start()
+
+    def stop(self):
+        if self._t is not None:
+            self._stop.set()
+            self._t.join(timeout=2)
+        return self.samples
+
+
 class ClockSampler:
-    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+    """nvidia-smi samples of SM clock and throttle reasons during a region
+    (plus NvmlReader's ~1 ms samples of the same quantities)."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -96,8 +146,10 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.path = None
+        self.nvml = NvmlReader(index)
 
     def start(self):
+        self.nvml.start()
         try:
             import tempfile
             fd, self.path = tempfile.mkstemp(suffix=".csv")
@@ -116,8 +168,9 @@ class ClockSampler:
             self.proc = None
 
     def stop(self):
+        fine = self.nvml.stop()
         if self.proc is None:
-            return None
+            return self._summary([], fine)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -142,10 +195,15 @@ class ClockSampler:
                 continue
             (inside if start >= first else before).append(rec)
         use = inside or before[-1:]  # a region shorter than the interval: the last sample
+        return self._summary(use, fine, len(inside))
+
+    @staticmethod
+    def _summary(smi, fine, smi_inside=0):
+        use = smi + fine
         if not use:
             return None
         return {"sm_mhz": statistics.median(r[0] for r in use), "sm_max_mhz": max(r[1] for r in use),
-                "samples": len(inside), "interval_ms": 20,
+                "samples": smi_inside, "interval_ms": 20, "nvml_samples": len(fine),
                 "reasons": sorted(set().union(*(r[2] for r in use)))}
 
 
