@@ -12,7 +12,10 @@ segtaco_spmm), operands resident in HBM.  `value` = algorithmic bytes per
 step / device time per step, where algorithmic bytes = nnz*(4+4) + (M+1)*4 +
 K*N*4 + M*N*4 (index + value streams, row_ptr, B read once, C written once).
 `roofline` is the same byte count over the product kernel's own event-timed
-duration, against the measured HBM copy bandwidth.  `e2e` runs the drop-in
+duration, against the measured HBM copy bandwidth; its `traffic` is the DRAM
+bytes ncu measured for one launch (profiles/traffic.json), and
+`traffic_GBps` / `traffic_frac` that traffic over the same duration.  `clocks`
+comes from nvidia-smi and ~1 ms NVML samples during the timed region.  `e2e` runs the drop-in
 entry point (segtaco_taco_call, segTACO's spmm_* surface) on pinned host
 operands: copies in, product, copy out, per step.  `cpu_baseline` times the
 oracle's restatement of segTACO's CPU product (Eigen's row-parallel order) on
