@@ -109,9 +109,12 @@ int run_spmm_planned(const SpmmPlan &plan, int M, int K, long long nnz, const in
                      bool partition_ready = false);
 
 // ---- side ops (sddmm.cu, spmspv.cu; SpMV runs the SpMM kernel with N = 1) ----
+// `starts_ready`: `starts` already holds the block starts of this row_ptr (a
+// cached matrix), so only the product is launched.
 int launch_sddmm(int M, long long nnz, const int *row_ptr, const int *col, const float *val,
                  const void *X, const void *Y, int x_dtype, long long ldx, long long ldy, int D,
-                 float *out, int *starts, int P, long long nblk, cudaStream_t s);
+                 float *out, int *starts, int P, long long nblk, cudaStream_t s,
+                 bool starts_ready = false);
 int launch_spmspv(int M, int K, const int *col_ptr, const int *row_idx, const float *val, int nx,
                   const int *x_idx, const float *x_vals, float *y, cudaStream_t s);
 

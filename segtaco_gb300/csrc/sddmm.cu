@@ -222,10 +222,12 @@ __global__ void __launch_bounds__(kCta, 4) sddmm_fixed_kernel(
 
 int launch_sddmm(int M, long long nnz, const int *row_ptr, const int *col, const float *val,
                  const void *X, const void *Y, int x_dtype, long long ldx, long long ldy, int D,
-                 float *out, int *starts, int P, long long nblk, cudaStream_t s) {
+                 float *out, int *starts, int P, long long nblk, cudaStream_t s,
+                 bool starts_ready) {
   if (nnz == 0) return SEGTACO_OK;
   (void)P;
-  SEGTACO_TRY(launch_block_starts_canonical(row_ptr, M, kSddmmBlock, nblk, starts, s));
+  if (!starts_ready)
+    SEGTACO_TRY(launch_block_starts_canonical(row_ptr, M, kSddmmBlock, nblk, starts, s));
   const dim3 grid((unsigned)((nblk + (kCta / 32) - 1) / (kCta / 32)));
   // Vector width: 16-byte loads when D and the strides allow it.
   const int esz = x_dtype == SEGTACO_BF16 ? 2 : 4;

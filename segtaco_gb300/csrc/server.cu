@@ -55,6 +55,7 @@ struct Matrix {
   const float *h_val = nullptr;
   long long max_row = 0;
   size_t bytes = 0, off_col = 0, off_val = 0;
+  size_t off_starts = 0;  // SDDMM block starts of row_ptr, computed at upload
   // Residency: touched by the scheduler thread only.
   char *dmem = nullptr;
   bool resident = false;
@@ -308,6 +309,14 @@ void segtaco_server::launch(Slot &sl, std::vector<Req *> &take, std::vector<Matr
       st = copy(m->dmem + m->off_col, m->h_col, (size_t)m->nnz * 4, cudaMemcpyHostToDevice, s);
     if (st == SEGTACO_OK && m->nnz && m->h_val)
       st = copy(m->dmem + m->off_val, m->h_val, (size_t)m->nnz * 4, cudaMemcpyHostToDevice, s);
+    // The SDDMM block starts depend only on row_ptr: computed once here, so a
+    // resident matrix's SDDMM requests launch the product alone.
+    if (st == SEGTACO_OK && m->nnz && !fake) {
+      const long long P = sddmm_block_nnz();
+      st = launch_block_starts_canonical(reinterpret_cast<const int *>(m->dmem), m->M, (int)P,
+                                         (m->nnz + P - 1) / P,
+                                         reinterpret_cast<int *>(m->dmem + m->off_starts), s);
+    }
     if (!fake) {
       if (!m->ready) cudaEventCreateWithFlags(&m->ready, cudaEventDisableTiming);
       cudaEventRecord(m->ready, s);
@@ -411,8 +420,9 @@ void segtaco_server::launch(Slot &sl, std::vector<Req *> &take, std::vector<Matr
       const long long P = sddmm_block_nnz();
       const long long nblk = (m->nnz + P - 1) / P;
       const int st = launch_sddmm(m->M, m->nnz, rp, col, val, Bd, Yd, q->r.dtype, q->r.N,
-                                  q->r.N, q->r.N, outd, reinterpret_cast<int *>(scratch), (int)P,
-                                  nblk, s);
+                                  q->r.N, q->r.N, outd,
+                                  reinterpret_cast<int *>(m->dmem + m->off_starts), (int)P, nblk,
+                                  s, /*starts_ready=*/true);
       if (st != SEGTACO_OK) q->status = st;
     }
   }
@@ -585,8 +595,7 @@ int segtaco_server::submit_at(const segtaco_request &r, double t_arrival, int64_
       return set_error(SEGTACO_EINVAL, "server: X, Y or out is NULL");
     q->in_bytes = align256((size_t)m->M * r.N * es) + (size_t)m->K * r.N * es;
     q->out_bytes = (size_t)m->nnz * 4;
-    const long long P = sddmm_block_nnz();
-    q->scratch_bytes = align256((size_t)((m->nnz + P - 1) / P + 1) * 4);
+    q->scratch_bytes = 0;  // block starts live with the cached matrix
   }
   if (on_device) {
     q->in_bytes = 0;  // nothing staged: staged() counts only scratch
@@ -682,7 +691,11 @@ int segtaco_server_add_matrix(segtaco_server *S, int64_t id, int32_t M, int32_t 
   m->max_row = max_row;
   m->off_col = align256((size_t)(M + 1) * 4);
   m->off_val = m->off_col + align256((size_t)nnz * 4);
-  m->bytes = m->off_val + (vals ? align256((size_t)nnz * 4) : 0);
+  m->off_starts = m->off_val + (vals ? align256((size_t)nnz * 4) : 0);
+  {
+    const long long P = sddmm_block_nnz();
+    m->bytes = m->off_starts + align256((size_t)((nnz + P - 1) / P + 1) * 4);
+  }
   std::lock_guard<std::mutex> lk(S->mu);
   if (S->mats.count(id)) return set_error(SEGTACO_EINVAL, "server: matrix id %lld exists", (long long)id);
   S->mats.emplace(id, std::move(m));
