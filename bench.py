@@ -858,6 +858,8 @@ def run_ours(args, world, rank, local):
                          "traffic": traffic, "kernel": kernel_name,
                          "gathered_bytes": A.nnz * N * 4,
                          "gather_GBps": round(A.nnz * N * 4 / kern_ms / 1e6, 1),
+                         "flops": 2 * A.nnz * N,
+                         "tflops": round(2 * A.nnz * N / kern_ms / 1e9, 3),
                          "kernel_ms": round(kern_ms, 4), "peak_source": peak_kind + " hbm_gbs",
                          # the DRAM bytes ncu measured per launch over the live kernel time:
                          # how close the kernel runs to HBM for the traffic it causes
