@@ -152,7 +152,6 @@ class ClockSampler:
         self.nvml = NvmlReader(index)
 
     def start(self):
-        self.nvml.start()
         try:
             import tempfile
             fd, self.path = tempfile.mkstemp(suffix=".csv")
@@ -169,6 +168,8 @@ class ClockSampler:
             self.first = os.path.getsize(self.path)
         except Exception:
             self.proc = None
+        # last, so that its samples start with the timed region
+        self.nvml.start()
 
     def stop(self):
         fine = self.nvml.stop()
