@@ -6,7 +6,8 @@ stand-ins for segTACO's SuiteSparse sweep), against the FP64 oracle:
 * banded-plus-random 262,144 x 262,144 (|i - j| <= 32 plus 8 random columns
   per row, 19,135,456 nonzeros), D = N = 64: SDDMM with fp32 and bf16 dense
   operands (every output), and the bf16-B SpMM (every element of C);
-* SpMSpV on the 1M x 1M power-law matrix stored by columns, x 10 % nonzero.
+* SpMSpV on the 1M x 1M power-law matrix stored by columns, x 10 % nonzero;
+* C and SDDMM's X past 2^31 elements (20M x 128).
 
 The 1M x 1M power-law SpMM and SpMV at full size are in test_gpu_spmm.py and
 test_gpu_side_ops.py; the 256-matrix pool in test_gpu_batch.py."""
@@ -79,3 +80,39 @@ def test_banded_bf16_spmm_full(cuda, banded):
     ops.spmm(dev(A), to_torch_bf16(bits), C_out=C)
     torch.cuda.synchronize()
     assert_spmm_close(C.cpu().numpy(), A, bits, bf16=True)
+
+
+def test_beyond_2g_elements(cuda):
+    """C (and SDDMM's X) with more than 2^31 elements: A 20,000,000 x 4,096
+    with one nonzero per row, N = D = 128, so offsets past 2^31 are reached
+    by the rows at the end.  One product per element makes every schedule's
+    result bit-exact (fp32 val * b); sampled rows include the last ones."""
+    M, K, NC = 20_000_000, 4096, 128
+    assert M * NC > 2**31
+    rng = np.random.default_rng(0)
+    col = rng.integers(0, K, M).astype(np.int32)
+    val = rng.uniform(-1, 1, M).astype(np.float32)
+    A = synth.CSR(np.arange(M + 1, dtype=np.int32), col, val, M, K)
+    B = synth.dense(K, NC, seed=1)
+    Ad, Bd = dev(A), torch.from_numpy(B).cuda()
+    rows = np.unique(np.concatenate([np.arange(4), np.arange(M - 4, M),
+                                     rng.integers(2**31 // NC, M, 200), rng.integers(0, M, 100)]))
+    rows_d = torch.from_numpy(rows).cuda()
+    want = val[rows, None] * B[col[rows]]  # fp32 products, one rounding each
+    C = torch.empty((M, NC), device="cuda")
+    for sched in ("rb_sr", "rb_pr", "eb_sr", "eb_pr"):
+        C.fill_(float("nan"))
+        ops.spmm(Ad, Bd, C_out=C, config=N.Config.make(schedule=sched))
+        torch.cuda.synchronize()
+        assert np.array_equal(C[rows_d].cpu().numpy(), want), sched
+    del C
+    g = torch.Generator(device="cuda").manual_seed(3)
+    X = torch.rand((M, NC), device="cuda", generator=g) * 2 - 1
+    Y = torch.from_numpy(synth.dense(K, NC, seed=4)).cuda()
+    out = ops.sddmm(Ad, X, Y)
+    torch.cuda.synchronize()
+    Xr = X[rows_d].double().cpu().numpy()
+    Yr = Y.double().cpu().numpy()[col[rows]]
+    ref = val[rows].astype(np.float64) * (Xr * Yr).sum(axis=1)
+    bound = np.abs(val[rows].astype(np.float64)) * np.abs(Xr * Yr).sum(axis=1)
+    assert O.max_bound_err(out[rows_d].cpu().numpy(), ref, bound) <= TOL
