@@ -109,6 +109,31 @@ int run_spmm_planned(const SpmmPlan &plan, int M, int K, long long nnz, const in
                      bool partition_ready = false);
 
 // ---- side ops (sddmm.cu, spmspv.cu; SpMV runs the SpMM kernel with N = 1) ----
+// One SDDMM problem of a multi-problem launch (device array): block b of the
+// launch with blk_begin <= b < blk_begin + ceil(nnz / sddmm_block_nnz()).
+struct SddmmProblem {
+  int M;
+  long long nnz;
+  const int *row_ptr, *col;
+  const float *val;
+  const void *X, *Y;
+  long long ldx, ldy;
+  float *out;
+  const int *starts;  // block starts of row_ptr (sddmm_block_nnz() nonzeros each)
+  long long blk_begin;
+};
+// Kernel shape of an SDDMM: family 0 = the general kernel (V-wide vectors),
+// 1 = fp32 32-byte lanes, 2 = bf16 32-byte lanes, 3 = 16-byte lanes; problems
+// of one non-zero family and (KI, G) can share a multi-problem launch.
+struct SddmmShape {
+  int family = 0, KI = 0, G = 0, V = 1;
+};
+SddmmShape sddmm_shape(int x_dtype, int D, long long ldx, long long ldy, const void *X,
+                       const void *Y);
+// One launch over `nprobs` problems of the fixed shape `sh` (device array
+// `probs`, blocks 0 .. total_blocks - 1); their block starts must be ready.
+int launch_sddmm_multi(const SddmmShape &sh, int x_dtype, const SddmmProblem *probs, int nprobs,
+                       long long total_blocks, cudaStream_t s);
 // `starts_ready`: `starts` already holds the block starts of this row_ptr (a
 // cached matrix), so only the product is launched.
 int launch_sddmm(int M, long long nnz, const int *row_ptr, const int *col, const float *val,

@@ -126,18 +126,16 @@ __global__ void __launch_bounds__(kCta, 3) sddmm_kernel(int M, long long nnz,
 // per step.  A group keeps its slice of X[i] in registers until its row
 // changes.  Raw vectors stay in registers until their multiply-adds.
 template <typename XT, int V, int G, int KI>
-__global__ void __launch_bounds__(kCta, 4) sddmm_fixed_kernel(
+__device__ __forceinline__ void sddmm_fixed_block(
     int M, long long nnz, const int *__restrict__ row_ptr, const int *__restrict__ col,
     const float *__restrict__ val, const XT *__restrict__ X, const XT *__restrict__ Y,
     long long ldx, long long ldy, float *__restrict__ out, const int *__restrict__ starts,
-    long long nblk) {
+    long long w) {
   constexpr int P = 32 / G;
   using Dv = Dense<XT, V>;
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int g = lane / G, gl = lane & (G - 1);
-  const long long w = (long long)blockIdx.x * (kCta / 32) + threadIdx.x / 32;
-  if (w >= nblk) return;
   const uint64_t pol = l2_policy_evict_normal();
   const long long pb = w * kSddmmBlock;
   const long long pe = pb + kSddmmBlock < nnz ? pb + kSddmmBlock : nnz;
@@ -212,6 +210,139 @@ __global__ void __launch_bounds__(kCta, 4) sddmm_fixed_kernel(
   }
 }
 
+template <typename XT, int V, int G, int KI>
+__global__ void __launch_bounds__(kCta, 4) sddmm_fixed_kernel(
+    int M, long long nnz, const int *__restrict__ row_ptr, const int *__restrict__ col,
+    const float *__restrict__ val, const XT *__restrict__ X, const XT *__restrict__ Y,
+    long long ldx, long long ldy, float *__restrict__ out, const int *__restrict__ starts,
+    long long nblk) {
+  const long long w = (long long)blockIdx.x * (kCta / 32) + threadIdx.x / 32;
+  if (w >= nblk) return;  // whole warp leaves together
+  sddmm_fixed_block<XT, V, G, KI>(M, nnz, row_ptr, col, val, X, Y, ldx, ldy, out, starts, w);
+}
+
+// Several problems of one shape in one launch: warp w takes block
+// w - blk_begin[p] of the last problem p with blk_begin[p] <= w.
+template <typename XT, int V, int G, int KI>
+__global__ void __launch_bounds__(kCta, 4) sddmm_fixed_multi_kernel(
+    const SddmmProblem *__restrict__ probs, int nprobs, long long total) {
+  const long long w = (long long)blockIdx.x * (kCta / 32) + threadIdx.x / 32;
+  if (w >= total) return;  // whole warp leaves together
+  int lo = 0, hi = nprobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (probs[mid].blk_begin <= w)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const SddmmProblem &a = probs[lo];
+  sddmm_fixed_block<XT, V, G, KI>(a.M, a.nnz, a.row_ptr, a.col, a.val,
+                                  static_cast<const XT *>(a.X), static_cast<const XT *>(a.Y),
+                                  a.ldx, a.ldy, a.out, a.starts, w - a.blk_begin);
+}
+
+// Fixed shapes (KI, G) of each family, for both launches.
+#define SEGTACO_SDDMM_SHAPES32(X_) X_(1, 1) X_(1, 2) X_(1, 4) X_(2, 4) X_(2, 8) X_(2, 16)
+#define SEGTACO_SDDMM_SHAPES16(X_) \
+  X_(1, 1) X_(2, 1) X_(4, 1) X_(4, 2) X_(4, 4) X_(4, 8) X_(4, 16) X_(4, 32)
+
+// Fixed shape of an SDDMM (shared by the single and the multi-problem launch):
+// family 1 = fp32 32-byte lanes (V = 8), 2 = bf16 32-byte lanes (V = 16),
+// 3 = 16-byte lanes (V = 16 / element size), 0 = the general kernel.
+SddmmShape sddmm_shape(int x_dtype, int D, long long ldx, long long ldy, const void *X,
+                       const void *Y) {
+  SddmmShape sh;
+  const int esz = x_dtype == SEGTACO_BF16 ? 2 : 4;
+  const uintptr_t al = (uintptr_t)X | (uintptr_t)Y;
+  int V = 16 / esz;
+  while (V > 1 && (D % V != 0 || ldx % V != 0 || ldy % V != 0 || (al % (V * esz)) != 0)) V >>= 1;
+  sh.V = V;
+  // 32-byte lanes (one ld.global.v8), G >= 4 lanes reading whole 128-byte lines
+  // of a row per load instruction (16-byte lanes read each line of Y in two
+  // halves, and the kernel is bound by the L1 data pipe); KI <= 2 loads per
+  // lane keep the variants within 64 registers.
+  const int w32 = 32 / esz;
+  if (V * esz == 16 && D % w32 == 0 && ldx % w32 == 0 && ldy % w32 == 0 && (al % 32) == 0) {
+    const int T = D / w32;
+    if (T >= 1 && T <= 32 && (T & (T - 1)) == 0) {
+      sh.family = esz == 4 ? 1 : 2;
+      sh.G = T < 4 ? T : (T / 2 > 4 ? T / 2 : 4);
+      sh.KI = T / sh.G;
+      return sh;
+    }
+  }
+  // Sixteen-byte vectors with D / V a power of two up to 128 (KI <= 4 loads).
+  if (V * esz == 16 && D % V == 0) {
+    const int T = D / V;
+    if (T >= 1 && T <= 128 && (T & (T - 1)) == 0) {
+      sh.family = 3;
+      sh.KI = T < 4 ? T : 4;
+      sh.G = T / sh.KI;
+    }
+  }
+  return sh;
+}
+
+namespace {
+
+// Fixed shapes (KI, G) of each family.
+#define SEGTACO_SDDMM_SHAPES32(X_) X_(1, 1) X_(1, 2) X_(1, 4) X_(2, 4) X_(2, 8) X_(2, 16)
+#define SEGTACO_SDDMM_SHAPES16(X_) \
+  X_(1, 1) X_(2, 1) X_(4, 1) X_(4, 2) X_(4, 4) X_(4, 8) X_(4, 16) X_(4, 32)
+// Switch over the family's shapes, each case launching CASE_(XT, V, KI, G).
+#define SEGTACO_SDDMM_SWITCH(sh, x_dtype)                                                  \
+  switch ((sh).family * 10000 + (sh).KI * 100 + (sh).G) {                                \
+    SEGTACO_SDDMM_SHAPES32(SEGTACO_SDDMM_F1) SEGTACO_SDDMM_SHAPES32(SEGTACO_SDDMM_F2)     \
+    default:                                                                             \
+      if ((sh).family == 3 && (x_dtype) == SEGTACO_BF16) {                               \
+        switch ((sh).KI * 100 + (sh).G) {                                                \
+          SEGTACO_SDDMM_SHAPES16(SEGTACO_SDDMM_F3B)                                      \
+          default: return set_error(SEGTACO_EUNSUPPORTED, "sddmm: no fixed shape");      \
+        }                                                                                \
+      } else if ((sh).family == 3) {                                                     \
+        switch ((sh).KI * 100 + (sh).G) {                                                \
+          SEGTACO_SDDMM_SHAPES16(SEGTACO_SDDMM_F3F)                                      \
+          default: return set_error(SEGTACO_EUNSUPPORTED, "sddmm: no fixed shape");      \
+        }                                                                                \
+      } else {                                                                           \
+        return set_error(SEGTACO_EUNSUPPORTED, "sddmm: no fixed shape");                 \
+      }                                                                                  \
+  }
+#define SEGTACO_SDDMM_F1(KI_, G_) \
+  case 10000 + KI_ * 100 + G_: CASE_(float, 8, KI_, G_) break;
+#define SEGTACO_SDDMM_F2(KI_, G_) \
+  case 20000 + KI_ * 100 + G_: CASE_(uint16_t, 16, KI_, G_) break;
+#define SEGTACO_SDDMM_F3B(KI_, G_) \
+  case KI_ * 100 + G_: CASE_(uint16_t, 8, KI_, G_) break;
+#define SEGTACO_SDDMM_F3F(KI_, G_) \
+  case KI_ * 100 + G_: CASE_(float, 4, KI_, G_) break;
+
+int launch_fixed_single(const SddmmShape &sh, int x_dtype, dim3 grid, int M, long long nnz,
+                        const int *row_ptr, const int *col, const float *val, const void *X,
+                        const void *Y, long long ldx, long long ldy, float *out, const int *starts,
+                        long long nblk, cudaStream_t s) {
+#define CASE_(XT, V, KI, G)                                                                \
+  sddmm_fixed_kernel<XT, V, G, KI><<<grid, kCta, 0, s>>>(M, nnz, row_ptr, col, val,       \
+                                                         static_cast<const XT *>(X),      \
+                                                         static_cast<const XT *>(Y), ldx, \
+                                                         ldy, out, starts, nblk);
+  SEGTACO_SDDMM_SWITCH(sh, x_dtype)
+#undef CASE_
+  return check_launch("sddmm_fixed_kernel");
+}
+
+int launch_fixed_multi(const SddmmShape &sh, int x_dtype, dim3 grid, const SddmmProblem *probs,
+                       int nprobs, long long total, cudaStream_t s) {
+#define CASE_(XT, V, KI, G) \
+  sddmm_fixed_multi_kernel<XT, V, G, KI><<<grid, kCta, 0, s>>>(probs, nprobs, total);
+  SEGTACO_SDDMM_SWITCH(sh, x_dtype)
+#undef CASE_
+  return check_launch("sddmm_fixed_multi_kernel");
+}
+
+}  // namespace
+
 #define SEGTACO_SDDMM_CASE(XT, V, G)                                                          \
   case V * 100 + G:                                                                           \
     sddmm_kernel<XT, V, G><<<grid, kCta, 0, s>>>(M, nnz, row_ptr, col, val,                   \
@@ -229,80 +360,13 @@ int launch_sddmm(int M, long long nnz, const int *row_ptr, const int *col, const
   if (!starts_ready)
     SEGTACO_TRY(launch_block_starts_canonical(row_ptr, M, kSddmmBlock, nblk, starts, s));
   const dim3 grid((unsigned)((nblk + (kCta / 32) - 1) / (kCta / 32)));
-  // Vector width: 16-byte loads when D and the strides allow it.
-  const int esz = x_dtype == SEGTACO_BF16 ? 2 : 4;
-  const uintptr_t al = (uintptr_t)X | (uintptr_t)Y;
-  int V = 16 / esz;
-  while (V > 1 && (D % V != 0 || ldx % V != 0 || ldy % V != 0 || (al % (V * esz)) != 0)) V >>= 1;
-  // fp32 with D a multiple of 8 and 32-byte aligned rows: 32-byte lanes (one
-  // ld.global.v8.f32), G >= 4 lanes reading whole 128-byte lines of a row per
-  // load instruction (16-byte lanes read each line of Y in two halves, and the
-  // kernel is bound by the L1 data pipe); KI <= 2 loads per lane keep the
-  // variants within 64 registers.
-  if (esz == 4 && V == 4 && D % 8 == 0 && ldx % 8 == 0 && ldy % 8 == 0 && (al % 32) == 0) {
-    const int T = D / 8;
-    if (T >= 1 && T <= 32 && (T & (T - 1)) == 0) {
-      const int Gf = T < 4 ? T : (T / 2 > 4 ? T / 2 : 4), KI = T / Gf;
-#define SEGTACO_SDDMM_FIXED8(KI_, G_)                                                        \
-  case KI_ * 100 + G_:                                                                       \
-    sddmm_fixed_kernel<float, 8, G_, KI_><<<grid, kCta, 0, s>>>(                             \
-        M, nnz, row_ptr, col, val, static_cast<const float *>(X),                            \
-        static_cast<const float *>(Y), ldx, ldy, out, starts, nblk);                         \
-    return check_launch("sddmm_fixed_kernel");
-      switch (KI * 100 + Gf) {
-        SEGTACO_SDDMM_FIXED8(1, 1) SEGTACO_SDDMM_FIXED8(1, 2) SEGTACO_SDDMM_FIXED8(1, 4)
-        SEGTACO_SDDMM_FIXED8(2, 4) SEGTACO_SDDMM_FIXED8(2, 8) SEGTACO_SDDMM_FIXED8(2, 16)
-        default: break;
-      }
-#undef SEGTACO_SDDMM_FIXED8
-    }
-  }
-  // bf16 with D a multiple of 16 and 32-byte aligned rows: 32-byte lanes of 16
-  // values (ld.global.v8.b32), G >= 4 lanes per whole 128-byte line.
-  if (esz == 2 && V == 8 && D % 16 == 0 && ldx % 16 == 0 && ldy % 16 == 0 && (al % 32) == 0) {
-    const int T = D / 16;
-    if (T >= 1 && T <= 32 && (T & (T - 1)) == 0) {
-      const int Gf = T < 4 ? T : (T / 2 > 4 ? T / 2 : 4), KI = T / Gf;
-#define SEGTACO_SDDMM_FIXED16(KI_, G_)                                                       \
-  case KI_ * 100 + G_:                                                                       \
-    sddmm_fixed_kernel<uint16_t, 16, G_, KI_><<<grid, kCta, 0, s>>>(                         \
-        M, nnz, row_ptr, col, val, static_cast<const uint16_t *>(X),                         \
-        static_cast<const uint16_t *>(Y), ldx, ldy, out, starts, nblk);                      \
-    return check_launch("sddmm_fixed_kernel");
-      switch (KI * 100 + Gf) {
-        SEGTACO_SDDMM_FIXED16(1, 1) SEGTACO_SDDMM_FIXED16(1, 2) SEGTACO_SDDMM_FIXED16(1, 4)
-        SEGTACO_SDDMM_FIXED16(2, 4) SEGTACO_SDDMM_FIXED16(2, 8) SEGTACO_SDDMM_FIXED16(2, 16)
-        default: break;
-      }
-#undef SEGTACO_SDDMM_FIXED16
-    }
-  }
-  // Sixteen-byte vectors with D / V a power of two up to 128: the fixed-shape
-  // kernel (KI vector loads per lane, at most 4).
-  if (V * esz == 16 && D % V == 0) {
-    const int T = D / V;
-    if (T >= 1 && T <= 128 && (T & (T - 1)) == 0) {
-      const int KI = T < 4 ? T : 4, Gf = T / KI;
-      const int key = KI * 100 + Gf;
-#define SEGTACO_SDDMM_FIXED(XT, KI_, G_)                                                    \
-  case KI_ * 100 + G_:                                                                       \
-    sddmm_fixed_kernel<XT, 16 / sizeof(XT), G_, KI_><<<grid, kCta, 0, s>>>(                  \
-        M, nnz, row_ptr, col, val, static_cast<const XT *>(X), static_cast<const XT *>(Y), ldx, \
-        ldy, out, starts, nblk);                                                             \
-    return check_launch("sddmm_fixed_kernel");
-#define SEGTACO_SDDMM_FIXED_ALL(XT)                                                          \
-  SEGTACO_SDDMM_FIXED(XT, 1, 1) SEGTACO_SDDMM_FIXED(XT, 2, 1) SEGTACO_SDDMM_FIXED(XT, 4, 1) \
-  SEGTACO_SDDMM_FIXED(XT, 4, 2) SEGTACO_SDDMM_FIXED(XT, 4, 4) SEGTACO_SDDMM_FIXED(XT, 4, 8) \
-  SEGTACO_SDDMM_FIXED(XT, 4, 16) SEGTACO_SDDMM_FIXED(XT, 4, 32)
-      if (x_dtype == SEGTACO_BF16) {
-        switch (key) { SEGTACO_SDDMM_FIXED_ALL(uint16_t) default: break; }
-      } else {
-        switch (key) { SEGTACO_SDDMM_FIXED_ALL(float) default: break; }
-      }
-#undef SEGTACO_SDDMM_FIXED_ALL
-#undef SEGTACO_SDDMM_FIXED
-    }
-  }
+  // The fixed-shape kernel where D and the operands allow it; the general
+  // kernel (V-wide vectors, G lanes covering D) otherwise.
+  const SddmmShape sh = sddmm_shape(x_dtype, D, ldx, ldy, X, Y);
+  if (sh.family != 0)
+    return launch_fixed_single(sh, x_dtype, grid, M, nnz, row_ptr, col, val, X, Y, ldx, ldy, out,
+                               starts, nblk, s);
+  const int V = sh.V;
   // Lanes per dot product: enough to cover D in one pass, at most 32.
   int G = 1;
   while (G < 32 && G * V < D) G <<= 1;
@@ -339,6 +403,14 @@ int launch_sddmm(int M, long long nnz, const int *row_ptr, const int *col, const
     }
   }
   return check_launch("sddmm_kernel");
+}
+
+int launch_sddmm_multi(const SddmmShape &sh, int x_dtype, const SddmmProblem *probs, int nprobs,
+                      long long total_blocks, cudaStream_t s) {
+  if (total_blocks <= 0 || nprobs <= 0) return SEGTACO_OK;
+  if (sh.family == 0) return set_error(SEGTACO_EUNSUPPORTED, "sddmm: no fixed shape to batch");
+  const dim3 grid((unsigned)((total_blocks + (kCta / 32) - 1) / (kCta / 32)));
+  return launch_fixed_multi(sh, x_dtype, grid, probs, nprobs, total_blocks, s);
 }
 
 long long sddmm_block_nnz() { return kSddmmBlock; }

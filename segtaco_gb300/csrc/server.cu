@@ -327,6 +327,14 @@ void segtaco_server::launch(Slot &sl, std::vector<Req *> &take, std::vector<Matr
   std::vector<segtaco_spmm_problem> probs;
   std::vector<SpmmPlan> plans;
   std::vector<Req *> spmm_reqs;
+  // SDDMM requests of one fixed kernel shape and dtype share one launch.
+  struct SddmmGroup {
+    SddmmShape sh;
+    int dtype = 0;
+    std::vector<SddmmProblem> probs;
+    std::vector<Req *> reqs;
+  };
+  std::vector<SddmmGroup> sddmm_groups;
   std::vector<Matrix *> waited;
   for (Req *q : take) {
     Matrix *m = q->m;
@@ -419,12 +427,70 @@ void segtaco_server::launch(Slot &sl, std::vector<Req *> &take, std::vector<Matr
     } else if (!fake && m->nnz > 0) {
       const long long P = sddmm_block_nnz();
       const long long nblk = (m->nnz + P - 1) / P;
-      const int st = launch_sddmm(m->M, m->nnz, rp, col, val, Bd, Yd, q->r.dtype, q->r.N,
-                                  q->r.N, q->r.N, outd,
-                                  reinterpret_cast<int *>(m->dmem + m->off_starts), (int)P, nblk,
-                                  s, /*starts_ready=*/true);
-      if (st != SEGTACO_OK) q->status = st;
+      const int *starts = reinterpret_cast<const int *>(m->dmem + m->off_starts);
+      const SddmmShape sh = sddmm_shape(q->r.dtype, q->r.N, q->r.N, q->r.N, Bd, Yd);
+      if (per_call || sh.family == 0) {
+        const int st = launch_sddmm(m->M, m->nnz, rp, col, val, Bd, Yd, q->r.dtype, q->r.N,
+                                    q->r.N, q->r.N, outd, const_cast<int *>(starts), (int)P,
+                                    nblk, s, /*starts_ready=*/true);
+        if (st != SEGTACO_OK) q->status = st;
+      } else {
+        SddmmGroup *g = nullptr;
+        for (SddmmGroup &x : sddmm_groups)
+          if (x.dtype == q->r.dtype && x.sh.family == sh.family && x.sh.KI == sh.KI &&
+              x.sh.G == sh.G)
+            g = &x;
+        if (!g) {
+          sddmm_groups.emplace_back();
+          g = &sddmm_groups.back();
+          g->sh = sh;
+          g->dtype = q->r.dtype;
+        }
+        SddmmProblem sp;
+        sp.M = m->M;
+        sp.nnz = m->nnz;
+        sp.row_ptr = rp;
+        sp.col = col;
+        sp.val = val;
+        sp.X = Bd;
+        sp.Y = Yd;
+        sp.ldx = q->r.N;
+        sp.ldy = q->r.N;
+        sp.out = outd;
+        sp.starts = starts;
+        sp.blk_begin = 0;
+        g->probs.push_back(sp);
+        g->reqs.push_back(q);
+      }
     }
+  }
+  // One launch per SDDMM group; its descriptors in stream-ordered device memory
+  // freed on the same stream after the launch.
+  for (SddmmGroup &g : sddmm_groups) {
+    const long long P = sddmm_block_nnz();
+    long long total = 0;
+    for (SddmmProblem &sp : g.probs) {
+      sp.blk_begin = total;
+      total += (sp.nnz + P - 1) / P;
+    }
+    int st = SEGTACO_OK;
+    if (g.probs.size() == 1) {
+      const SddmmProblem &sp = g.probs[0];
+      st = launch_sddmm(sp.M, sp.nnz, sp.row_ptr, sp.col, sp.val, sp.X, sp.Y, g.dtype,
+                        sp.ldx, sp.ldy, (int)sp.ldx, sp.out, const_cast<int *>(sp.starts), (int)P,
+                        total, s, /*starts_ready=*/true);
+    } else {
+      const size_t bytes = g.probs.size() * sizeof(SddmmProblem);
+      void *d = nullptr;
+      st = dev_alloc(&d, bytes, s);
+      if (st == SEGTACO_OK) st = copy(d, g.probs.data(), bytes, cudaMemcpyHostToDevice, s);
+      if (st == SEGTACO_OK)
+        st = launch_sddmm_multi(g.sh, g.dtype, static_cast<const SddmmProblem *>(d),
+                                (int)g.probs.size(), total, s);
+      if (d) dev_free(d, s);
+    }
+    if (st != SEGTACO_OK)
+      for (Req *q : g.reqs) q->status = st;
   }
   if (!probs.empty() && !fake) {
     BatchLayout L;

@@ -57,6 +57,38 @@ def test_server_spmm_sddmm_against_oracle(cuda):
         assert st["completed"] == len(jobs) and st["failed"] == 0
 
 
+def test_sddmm_requests_grouped_by_shape(cuda):
+    """SDDMM requests of one kernel shape and dtype in a batch share one
+    multi-problem launch: 24 requests (D in {16, 32, 64}, fp32 and bf16, four
+    matrices) released at once to one slot, every output against FP64."""
+    mats = pool(4, seed0=40)
+    with Server(slots=1, max_batch=64) as s:
+        for i, (A, _) in enumerate(mats):
+            s.add_matrix(i, A)
+        reqs, keep, checks = [], [], []
+        for i, (A, _) in enumerate(mats):
+            for D in (16, 32, 64):
+                for bf16 in (False, True):
+                    X = synth.dense(A.M, D, seed=300 + 10 * i + D)
+                    Y = synth.dense(A.K, D, seed=400 + 10 * i + D)
+                    if bf16:
+                        X, Y = synth.to_bf16_bits(X), synth.to_bf16_bits(Y)
+                    out = np.full(A.nnz, np.nan, np.float32)
+                    reqs.append(Server.request(N.OP_SDDMM, i, X, out, Y=Y))
+                    keep.append((X, Y, out))
+                    checks.append((A, X, Y, out, bf16))
+        tickets = s.replay(reqs, [0.0] * len(reqs), keep=keep)
+        for t in tickets:
+            assert s.wait(t, 60000) == N.OK
+        for A, X, Y, out, bf16 in checks:
+            ref, S = O.sddmm_f64(A.row_ptr, A.col, A.val, X, Y, bf16=bf16)
+            if A.nnz:
+                assert np.max(np.abs(out - ref) / np.maximum(S, 1e-30)) <= TOL
+        st = s.stats()
+        assert st["completed"] == len(reqs) and st["failed"] == 0
+        assert st["batches"] < len(reqs)  # requests shared batches
+
+
 def test_same_result_alone_and_in_the_mix(cuda):
     mats = pool(12, seed0=50)
     A0, n0 = mats[0]
