@@ -834,8 +834,8 @@ def run_ours(args, world, rank, local):
         ceiling = run_gather_ceiling(ops, stream)
         link = run_link_probe(stream)
 
-    cpu = None
-    if rank == 0 and not args.no_cpu:
+    cpu = None  # the CPU baseline runs at N = 1 only (rank 0 of a single rank)
+    if rank == 0 and world == 1 and not args.no_cpu:
         sec, Ms, nnzs, threads = cpu_spmm_timed(A, B, 2)
         cpu = {"value": round(byts * (nnzs / A.nnz) / sec / 1e9, 3), "unit": UNIT,
                "cores": threads, "kind": "port",
