@@ -62,6 +62,13 @@ void *Scratch::take(size_t bytes) {
 // ---------------------------------------------------------------------------
 static bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
 
+// rb_sr products below this many nonzeros walk every row in the row-block
+// kernel: the list pass and the fork would cost more than a long row there.
+constexpr long long kLongRowsMinNnz = 1000000;
+// Default long-row threshold.  Measured on GB300 (1M x 1M power law, N = 128,
+// Zipf 1.8 / 1.922): 1024: 2.33 / 1.45 ms, 2048: 2.27 / 1.44, 4096: 2.23 / 1.46.
+constexpr long long kLongRowDefault = 2048;
+
 int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, long long ldc,
               const void *B, const float *C, const segtaco_config *cfg, SpmmPlan *plan) {
   segtaco_config c{};
@@ -142,6 +149,8 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
   plan->items_per_unit = 0;
   plan->nchunks = (M + plan->rows_per_unit - 1) / plan->rows_per_unit;  // rb: row blocks
   plan->workspace = 0;
+  plan->long_row = 0;
+  plan->px_entries = plan->py_entries = 0;
   if (schedule == SEGTACO_EB_SR || schedule == SEGTACO_EB_PR) {
     long long D = c.items_per_unit > 0 ? c.items_per_unit : 512;
     if (D < 1) D = 1;
@@ -150,8 +159,25 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
     if (nch < 1) nch = 1;
     plan->items_per_unit = D;
     plan->nchunks = nch;
-    plan->workspace = 2 * align256((size_t)(nch + 1) * sizeof(int));
+    plan->px_entries = plan->py_entries = nch + 1;
+  } else if (schedule == SEGTACO_RB_SR && nnz >= kLongRowsMinNnz &&
+             !(c.flags & SEGTACO_FLAG_NO_LONG_ROWS) && plan->walk != 2 && !plan->use_tma) {
+    // Long rows to CTAs of their own (spmm_long.cu): their ring copies 16-byte
+    // chunks of B rows, so B, ldb and N must allow 16-byte pieces.
+    const int epc = 16 / esz;
+    if (N % epc == 0 && ldb % epc == 0 && ((uintptr_t)B % 16) == 0) {
+      long long T = c.items_per_unit > 0 ? c.items_per_unit : kLongRowDefault;
+      if (T > nnz) T = nnz;
+      long long hi, lo;
+      long_list_caps(nnz, T, &hi, &lo);
+      plan->long_row = (int)T;
+      plan->px_entries = hi + lo;
+      plan->py_entries = 4;  // the two parts' counts, 64-bit work queue
+    }
   }
+  if (plan->px_entries)
+    plan->workspace = align256((size_t)plan->px_entries * sizeof(int)) +
+                      align256((size_t)plan->py_entries * sizeof(int));
   (void)K;
   return SEGTACO_OK;
 }
@@ -190,6 +216,12 @@ int run_spmm_planned(const SpmmPlan &plan, int M, int K, long long nnz, const in
     case SEGTACO_RB_SR:
     case SEGTACO_RB_PR:
       if (L.use_tma) return bf16 ? launch_spmm_tma_bf16(L, true, s) : launch_spmm_tma_f32(L, true, s);
+      if (plan.long_row > 0) {
+        L.long_row = plan.long_row;
+        if (!partition_ready)
+          SEGTACO_TRY(launch_long_rows_list(row_ptr, M, nnz, plan.long_row, px, py, s));
+        return launch_spmm_long_rows(L, px, py, s);
+      }
       return bf16 ? launch_spmm_bf16_rows(L, s) : launch_spmm_f32_rows(L, s);
     case SEGTACO_EB_SR:
     case SEGTACO_EB_PR:
@@ -258,12 +290,11 @@ int segtaco_autotune_heuristic(int32_t M, int32_t K, int64_t nnz, int32_t N, int
     cfg->col_tile = 32 * (16 / esz);
   else
     cfg->col_tile = bbytes <= 48e6 ? (N <= 64 * 4 / esz ? N : 64 * 4 / esz) : 128 / esz;
-  // rb_sr walks its longest row in one warp per slab: with B beyond L2 and a
-  // row-length tail, 64-column fp32 slabs (two warps per long row) measured
-  // 4.37 -> 3.93 ms on the 1M x 1M power law, N = 128 (eb_sr stays at 128:
-  // 1.43 vs 1.50 ms).
-  if (schedule == SEGTACO_RB_SR && esz == 4 && bbytes > 48e6 && skewed && N > 64)
-    cfg->col_tile = 64;
+  // rb_sr from 1M nonzeros hands its long rows to CTAs of their own
+  // (spmm_long.cu); its row-block kernel then takes 128-column slabs also for
+  // bf16 (8-byte lanes).  Measured on GB300, 1M x 1M power law, N = 128:
+  // fp32 2.32 ms (64-column slabs: 2.45), bf16 2.29 ms (256: 2.52).
+  if (schedule == SEGTACO_RB_SR && nnz >= 1000000) cfg->col_tile = 128;
   // fp32 with B beyond L2 (32-column slabs): 8 columns per lane (one 32-byte
   // load, 4 lanes per 128-byte segment, 8 slots), so a warp step covers 8 rows
   // or 8 nonzeros instead of 4.  Measured on GB300: 1M x 1M power law (skewed
@@ -280,7 +311,8 @@ int segtaco_autotune_heuristic(int32_t M, int32_t K, int64_t nnz, int32_t N, int
   // with B in L2 (banded, N = 64) 8 stays faster (0.224 vs 0.235 ms).
   if (!sequential && esz == 2 && bbytes > 48e6 && N % 16 == 0 && (skewed || nnz >= 4000000))
     cfg->vec = 16;
-  cfg->items_per_unit = 512;
+  // eb: merge-path items per chunk; rb_sr: the long-row threshold.
+  cfg->items_per_unit = schedule == SEGTACO_RB_SR ? (int)kLongRowDefault : 512;
   cfg->rows_per_unit = schedule == SEGTACO_RB_PR || schedule == SEGTACO_RB_SR ? 4 : 1;
   cfg->depth = (schedule == SEGTACO_RB_SR || schedule == SEGTACO_RB_PR) ? 8 : 4;
   cfg->flags = 0;
@@ -316,8 +348,8 @@ int segtaco_spmm(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr, cons
   SEGTACO_TRY(scratch.reserve(plan.workspace));
   int *px = nullptr, *py = nullptr;
   if (plan.workspace) {
-    px = static_cast<int *>(scratch.take((plan.nchunks + 1) * sizeof(int)));
-    py = static_cast<int *>(scratch.take((plan.nchunks + 1) * sizeof(int)));
+    px = static_cast<int *>(scratch.take(plan.px_entries * sizeof(int)));
+    py = static_cast<int *>(scratch.take(plan.py_entries * sizeof(int)));
   }
   const bool ready = cfg && (cfg->flags & SEGTACO_FLAG_PARTITION_READY);
   if (ready && plan.workspace && !workspace)
@@ -339,8 +371,9 @@ int segtaco_spmm_partition(int32_t M, int32_t K, int64_t nnz, const int32_t *row
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   Scratch scratch(workspace, workspace_bytes, s);
   SEGTACO_TRY(scratch.reserve(plan.workspace));
-  int *px = static_cast<int *>(scratch.take((plan.nchunks + 1) * sizeof(int)));
-  int *py = static_cast<int *>(scratch.take((plan.nchunks + 1) * sizeof(int)));
+  int *px = static_cast<int *>(scratch.take(plan.px_entries * sizeof(int)));
+  int *py = static_cast<int *>(scratch.take(plan.py_entries * sizeof(int)));
+  if (plan.long_row > 0) return launch_long_rows_list(row_ptr, M, nnz, plan.long_row, px, py, s);
   return launch_merge_path(row_ptr, M, nnz, plan.items_per_unit, plan.nchunks, px, py, C, ldc, N,
                            s);
 }
@@ -434,8 +467,8 @@ int segtaco_spmv(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr, cons
   SEGTACO_TRY(scratch.reserve(plan.workspace));
   int *px = nullptr, *py = nullptr;
   if (plan.workspace) {
-    px = static_cast<int *>(scratch.take((plan.nchunks + 1) * sizeof(int)));
-    py = static_cast<int *>(scratch.take((plan.nchunks + 1) * sizeof(int)));
+    px = static_cast<int *>(scratch.take(plan.px_entries * sizeof(int)));
+    py = static_cast<int *>(scratch.take(plan.py_entries * sizeof(int)));
   }
   return run_spmm_planned(plan, M, K, nnz, row_ptr, col, vals, x, SEGTACO_F32, 1, y, 1, 1, px, py,
                           s);

@@ -75,6 +75,7 @@ struct SpmmLaunch {
   bool bulk_copies;            // ... with cp.async.bulk (TMA) rather than cp.async
   bool deep;                   // row walk: 8 sixteen-byte loads in flight per lane
   int walk;                    // kWalkRows / kWalkRowsDeep / kWalkFlat (spmm_kernels.cuh)
+  int long_row = 0;            // rb_sr: rows of >= long_row nonzeros go to spmm_long.cu
 };
 // One launcher per (dense type, unit kind); each switches over (V, G).
 int launch_spmm_f32_rows(const SpmmLaunch &L, cudaStream_t s);
@@ -98,6 +99,10 @@ struct SpmmPlan {
   bool bulk_copies;
   bool deep;
   int walk;                  // kWalkRows / kWalkRowsDeep / kWalkFlat
+  int long_row;              // rb_sr: long-row threshold (0: every row in the row-block kernel)
+  long long px_entries;      // int32 entries of the first workspace array (eb: chunk-edge
+                             // rows; rb_sr long rows: the list of long rows)
+  long long py_entries;      // ... of the second (eb: chunk-edge nonzeros; long rows: counters)
   size_t workspace;          // bytes
 };
 int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, long long ldc,
@@ -140,6 +145,21 @@ int launch_sddmm(int M, long long nnz, const int *row_ptr, const int *col, const
                  const void *X, const void *Y, int x_dtype, long long ldx, long long ldy, int D,
                  float *out, int *starts, int P, long long nblk, cudaStream_t s,
                  bool starts_ready = false);
+// ---- rb_sr long rows (spmm_long.cu) ----
+// The two parts of the long-row list for threshold T: rows of >= 8T nonzeros
+// (at most nnz / 8T of them) and rows of T .. 8T-1 (at most nnz / T).
+inline void long_list_caps(long long nnz, long long T, long long *hi, long long *lo) {
+  *hi = nnz / (8 * T) + 1;
+  *lo = nnz / T + 1;
+}
+// Lists the rows of >= long_row nonzeros into `list` (long_list_caps entries)
+// and their counts into counters[0..1] (`counters`: 4 int32, cleared here).
+int launch_long_rows_list(const int *row_ptr, int M, long long nnz, int long_row, int *list,
+                          int *counters, cudaStream_t s);
+// The long-row CTAs for the listed rows, on a side stream forked from `s`, and
+// the row-block kernel `L` (L.long_row set: it skips those rows) on `s`.
+int launch_spmm_long_rows(const SpmmLaunch &L, const int *list, int *counters, cudaStream_t s);
+
 int launch_spmspv(int M, int K, const int *col_ptr, const int *row_idx, const float *val, int nx,
                   const int *x_idx, const float *x_vals, float *y, cudaStream_t s);
 

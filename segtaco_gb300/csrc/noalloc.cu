@@ -75,9 +75,15 @@ extern "C" int segtaco_spmm_noalloc(int32_t M, int32_t K, int64_t nnz, const int
                      "segtaco_spmm_noalloc: PARTITION_READY is not supported (shared scratch)");
   SpmmPlan plan;
   SEGTACO_TRY(plan_spmm(M, K, nnz, N, b_dtype, ldb, ldc, B, C, cfg, &plan));
+  if (plan.long_row > 0 && plan.px_entries > kNoallocEntries) {
+    // the rb_sr long-row list would not fit: every row in the row-block kernel
+    plan.long_row = 0;
+    plan.px_entries = plan.py_entries = 0;
+    plan.workspace = 0;
+  }
   int *px = nullptr, *py = nullptr;
   if (plan.workspace) {
-    if (plan.nchunks + 1 > kNoallocEntries)
+    if (plan.px_entries > kNoallocEntries)
       return set_error(SEGTACO_EINVAL,
                        "segtaco_spmm_noalloc: %lld merge-path chunks exceed the fixed scratch of "
                        "%lld chunks (2 MiB); raise items_per_unit or use segtaco_spmm",

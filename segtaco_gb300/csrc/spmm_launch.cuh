@@ -27,6 +27,7 @@ template <typename BT> inline SpmmArgs<BT> make_spmm_args(const SpmmLaunch &L) {
   a.units = L.units;
   a.rows_per_unit = L.rows_per_unit;
   a.l2_hints = L.l2_hints ? 1 : 0;
+  a.long_row = L.long_row;
   return a;
 }
 

@@ -154,6 +154,23 @@ def test_workspace_and_heuristic(native_lib):
     assert L.segtaco_spmm_workspace_size(1000, 1000, 20000, 128, N.F32, C.byref(cfg),
                                          C.byref(out)) == N.OK
     assert out.value == 0
+    # rb_sr from 1M nonzeros: the list of rows of >= items_per_unit (2048)
+    # nonzeros in two parts (rows of >= 8 * 2048: at most nnz / 16384; the
+    # others: at most nnz / 2048) and the counters; none with NO_LONG_ROWS or
+    # when N is not a multiple of the 16-byte chunk
+    def ws(n, **kw):
+        c = N.Config.make(schedule="rb_sr", **kw)
+        assert L.segtaco_spmm_workspace_size(10**6, 10**6, 2 * 10**7, n, N.F32, C.byref(c),
+                                             C.byref(out)) == N.OK
+        return out.value
+
+    def want(T):
+        entries = 2 * 10**7 // (8 * T) + 1 + 2 * 10**7 // T + 1
+        return (entries * 4 + 255) // 256 * 256 + 256
+    assert ws(128) == want(2048)
+    assert ws(128, items_per_unit=512) == want(512)
+    assert ws(128, flags=N.FLAG_NO_LONG_ROWS) == 0
+    assert ws(126) == 0
     h = N.Config()
     h.schedule = -1
     assert L.segtaco_autotune_heuristic(16384, 16384, 262144, 32, N.F32, 16, C.byref(h)) == N.OK
@@ -175,11 +192,25 @@ def test_workspace_and_heuristic(native_lib):
     assert L.segtaco_autotune_heuristic(10**6, 10**6, 2 * 10**7, 128, N.BF16, 48679,
                                         C.byref(h)) == N.OK
     assert (h.col_tile, h.vec) == (64, 16)  # bf16 B beyond L2, skewed: 16 columns per lane
-    for sched, tile in ((N.RB_SR, 64), (N.EB_SR, 128)):  # sequential: 16-byte lanes, rb_sr
-        h.schedule = sched                               # halves its slab on skewed rows
+    for sched, tile, items in ((N.RB_SR, 128, 2048), (N.EB_SR, 128, 512)):
+        h.schedule = sched  # sequential: 16-byte lanes; rb_sr: long-row threshold 2048
         assert L.segtaco_autotune_heuristic(10**6, 10**6, 2 * 10**7, 128, N.F32, 48679,
                                             C.byref(h)) == N.OK
         assert h.schedule == sched and h.col_tile == tile and h.vec == 0
+        assert h.items_per_unit == items
+    h.schedule = N.RB_SR  # bf16 too: 128-column slabs (8-byte lanes) from 1M nonzeros
+    assert L.segtaco_autotune_heuristic(10**6, 10**6, 2 * 10**7, 128, N.BF16, 48679,
+                                        C.byref(h)) == N.OK
+    assert h.col_tile == 128
+
+
+def test_flag_constants_match_the_header():
+    """Every SEGTACO_FLAG_* of include/segtaco.h has the same value in native.py."""
+    text = open(os.path.join(ROOT, "include", "segtaco.h")).read()
+    flags = dict(re.findall(r"#define SEGTACO_(FLAG_[A-Z0-9_]+)\s+(\d+)u", text))
+    assert len(flags) >= 7
+    for name, value in flags.items():
+        assert getattr(N, name) == int(value), name
 
 
 def test_device_available_is_a_query(native_lib):

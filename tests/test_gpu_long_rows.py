@@ -1,0 +1,137 @@
+"""rb_sr's long rows.  From 1M nonzeros on, rows of at least items_per_unit
+(default 2048) nonzeros are summed by CTAs of their own that stage B row
+segments in shared memory, beside the row-block kernel on a forked stream.
+Every column stays one fmaf chain in storage order, so the result must be
+bit-identical to the one-warp walk (FLAG_NO_LONG_ROWS) and to the sequential
+FP32 FMA restatement of segTACO's serial row sum (spmm_rb_sr.h:187-243):
+across thresholds, widths (one and several column slabs, widths the 16-byte
+copies cannot take), bf16 B, unit values, offset B, the partition-ready
+split, and graph capture (the allocation-free entry point: test_zz_no_alloc.py)."""
+import numpy as np
+import pytest
+import torch
+
+from gpu_util import dev, to_torch_bf16
+from oracle import oracle as O
+from segtaco_gb300 import native as N
+from segtaco_gb300 import ops, synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def A():
+    """Short rows (~29 nonzeros, 10 % empty) plus rows of exactly 50,000 /
+    20,000 / 5,000 / 1,000 / 600 nonzeros, rows of 2047, 2048 and 2049 (the
+    default threshold's edge) and of 16,383 / 16,384 (where rows move to the
+    front of the work list); 1.1M nonzeros."""
+    rng = np.random.default_rng(41)
+    M, K = 41_000, 50_000
+    lengths = rng.binomial(64, 0.45, M)
+    lengths[rng.random(M) < 0.1] = 0
+    long_rows = {7: 50_000, 100: 20_000, 2_000: 5_000, 39_999: 600, 15_000: 2_047,
+                 15_001: 2_048, 15_002: 2_049, 0: 1_000, 30_000: 16_383, 30_001: 16_384}
+    for r in long_rows:
+        lengths[r] = 0
+    rows = np.repeat(np.arange(M, dtype=np.int64), lengths)
+    keys = [np.unique(rows * K + rng.integers(0, K, rows.size))]
+    keys += [r * K + np.sort(rng.choice(K, L, replace=False)) for r, L in long_rows.items()]
+    A = synth._from_keys(np.sort(np.concatenate(keys)), M, K, rng)
+    L = A.row_lengths()
+    assert A.nnz >= 1_000_000 and all(L[r] == n for r, n in long_rows.items())
+    return A
+
+
+def rowseq(A, B, val=None):
+    return O.spmm_f32_rowseq(A.row_ptr, A.col, A.val if val is None else val, B, fma=True)
+
+
+def run(Ad, Bd, n, **kw):
+    C_ = torch.full((Ad.M, n), float("nan"), device="cuda")
+    ops.spmm(Ad, Bd, C_out=C_, config=N.Config.make(schedule="rb_sr", **kw))
+    torch.cuda.synchronize()
+    return C_.cpu().numpy()
+
+
+@pytest.mark.parametrize("n", [128, 96, 64, 32, 8, 200, 126])
+def test_bit_identical_to_one_warp_walk(cuda, A, n):
+    B = synth.dense(A.K, n, seed=n)
+    Ad, Bd = dev(A), torch.from_numpy(B).cuda()
+    got = run(Ad, Bd, n)
+    assert np.array_equal(got, run(Ad, Bd, n, flags=N.FLAG_NO_LONG_ROWS))
+    assert np.array_equal(got, rowseq(A, B))
+
+
+@pytest.mark.parametrize("threshold", [1, 31, 512, 2_049, 5_000, 10**7])
+def test_thresholds(cuda, A, threshold):
+    B = synth.dense(A.K, 64, seed=3)
+    got = run(dev(A), torch.from_numpy(B).cuda(), 64, items_per_unit=threshold)
+    assert np.array_equal(got, rowseq(A, B))
+
+
+@pytest.mark.parametrize("n", [128, 64, 200])
+def test_bf16_dense_operand(cuda, A, n):
+    bits = synth.to_bf16_bits(synth.dense(A.K, n, seed=5))
+    Bf = (bits.astype(np.uint32) << 16).view(np.float32)  # the bf16 values, exactly
+    Ad, Bd = dev(A), to_torch_bf16(bits)
+    got = run(Ad, Bd, n)
+    assert np.array_equal(got, run(Ad, Bd, n, flags=N.FLAG_NO_LONG_ROWS))
+    assert np.array_equal(got, rowseq(A, Bf))
+
+
+def test_values_default_to_one(cuda, A):
+    B = synth.dense(A.K, 64, seed=6)
+    got = run(dev(A, with_values=False), torch.from_numpy(B).cuda(), 64)
+    assert np.array_equal(got, rowseq(A, B, np.ones_like(A.val)))
+
+
+@pytest.mark.parametrize("off", [4, 1])  # 16-byte aligned (long-row CTAs) and not
+def test_offset_dense_operand(cuda, A, off):
+    B = synth.dense(A.K, 64 + 8, seed=7)
+    Bd = torch.from_numpy(B).cuda()[:, off:off + 64]
+    got = run(dev(A), Bd, 64)
+    assert np.array_equal(got, rowseq(A, np.ascontiguousarray(B[:, off:off + 64])))
+
+
+def test_partition_ready_and_reruns(cuda, A):
+    """segtaco_spmm_partition lists the long rows once; products with
+    PARTITION_READY reuse the list (the work queue is cleared per launch)."""
+    B = synth.dense(A.K, 128, seed=8)
+    Ad, Bd = dev(A), torch.from_numpy(B).cuda()
+    cfg = N.Config.make(schedule="rb_sr")
+    ws = torch.empty(ops.spmm_workspace_size(Ad, 128, N.F32, cfg), dtype=torch.uint8,
+                     device="cuda")
+    assert ws.numel() > 0
+    C_ = torch.full((A.M, 128), float("nan"), device="cuda")
+    ops.spmm_partition(Ad, C_, cfg, ws)
+    ready = N.Config.make(schedule="rb_sr", flags=N.FLAG_PARTITION_READY)
+    want = rowseq(A, B)
+    for _ in range(3):
+        C_.fill_(float("nan"))
+        ops.spmm(Ad, Bd, C_out=C_, config=ready, workspace=ws)
+        torch.cuda.synchronize()
+        assert np.array_equal(C_.cpu().numpy(), want)
+
+
+def test_graph_capture(cuda, A):
+    """The fork to the side stream inside a captured graph, replayed."""
+    B = synth.dense(A.K, 128, seed=9)
+    Ad, Bd = dev(A), torch.from_numpy(B).cuda()
+    cfg = N.Config.make(schedule="rb_sr")
+    ws = torch.empty(ops.spmm_workspace_size(Ad, 128, N.F32, cfg), dtype=torch.uint8,
+                     device="cuda")
+    C_ = torch.empty((A.M, 128), device="cuda")
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        ops.spmm(Ad, Bd, C_out=C_, config=cfg, workspace=ws)  # creates the side stream
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        ops.spmm(Ad, Bd, C_out=C_, config=cfg, workspace=ws)
+    want = rowseq(A, B)
+    for _ in range(2):
+        C_.fill_(float("nan"))
+        g.replay()
+        torch.cuda.synchronize()
+        assert np.array_equal(C_.cpu().numpy(), want)
+

@@ -58,8 +58,9 @@ def test_spmv_writes_every_row(cuda, name):
     assert torch.all(y == 0)
 
 
-def test_spmv_full_power_law(cuda):
-    A = synth.power_law(seed=0)
+@pytest.mark.parametrize("zipf_s", [1.8, 1.922])
+def test_spmv_full_power_law(cuda, zipf_s):
+    A = synth.power_law(s=zipf_s, seed=0)
     x = synth.dense(A.K, 1, seed=2).reshape(-1)
     y = ops.spmv(dev(A), torch.from_numpy(x).cuda()).cpu().numpy()
     S = O.spmm_absbound(A.row_ptr, A.col, A.val, x.reshape(-1, 1)).reshape(-1)

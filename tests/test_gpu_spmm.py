@@ -217,11 +217,13 @@ def test_empty_matrix_and_zero_width(cuda):
     assert C.shape == (Ad.M, 0)
 
 
-def test_full_power_law_all_schedules(cuda):
-    """The 1,000,000 x 1,000,000 Zipf(1.8) workload with N = 128: row sums of C
-    against the FP64 product A (B 1), and 3000 sampled rows (including the
-    longest ones) against the FP64 oracle, for all four schedules."""
-    A = synth.power_law(seed=0)
+@pytest.mark.parametrize("zipf_s", [1.8, 1.922])
+def test_full_power_law_all_schedules(cuda, zipf_s):
+    """The 1,000,000 x 1,000,000 Zipf workload with N = 128 (exponent 1.8:
+    19.9M nonzeros; 1.922: 10.1M): row sums of C against the FP64 product
+    A (B 1), and 3000 sampled rows (including the longest ones) against the
+    FP64 oracle, for all four schedules."""
+    A = synth.power_law(s=zipf_s, seed=0)
     B = synth.dense(A.K, 128, seed=1)
     Ad, Bd = dev(A), torch.from_numpy(B).cuda()
     C = torch.empty((A.M, 128), device="cuda")

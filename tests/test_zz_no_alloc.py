@@ -56,3 +56,20 @@ def test_noalloc_rejects_problems_beyond_its_scratch(cuda):
         pytest.skip("matrix too small to overflow the fixed scratch")
     st = _noalloc(Ad, Bd, Cd, cfg)
     assert st == N.EINVAL and "fixed scratch" in N.last_error()
+
+
+def test_noalloc_rb_sr_long_rows(cuda):
+    """rb_sr from 1M nonzeros lists its long rows in the fixed scratch: the
+    result stays the sequential FMA order, call after call."""
+    from oracle import oracle as O
+    A = synth.power_law(60_000, 50_000, 1.8, 40_000, 0.02, seed=35)
+    assert A.nnz >= 1_000_000 and A.row_lengths().max() >= 512
+    B = synth.dense(A.K, 128, seed=36)
+    Ad, Bd = dev(A), torch.from_numpy(B).cuda()
+    want = O.spmm_f32_rowseq(A.row_ptr, A.col, A.val, B, fma=True)
+    cfg = N.Config.make(schedule="rb_sr")
+    for _ in range(2):
+        Cd = torch.full((A.M, 128), float("nan"), device="cuda")
+        assert _noalloc(Ad, Bd, Cd, cfg) == N.OK, N.last_error()
+        torch.cuda.synchronize()
+        assert np.array_equal(Cd.cpu().numpy(), want)
