@@ -773,7 +773,8 @@ def run_ours(args, world, rank, local):
         cfg.depth = args.depth
     if args.vec:
         cfg.vec = args.vec
-    ws_bytes = max(256, ops.spmm_workspace_size(Ad, N, N_.F32, cfg))
+    ws_need = ops.spmm_workspace_size(Ad, N, N_.F32, cfg)
+    ws_bytes = max(256, ws_need)
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
 
     # per-schedule sweep (context for the headline; same workload)
@@ -914,7 +915,9 @@ def run_ours(args, world, rank, local):
                          "traffic_GBps": (round(traffic / kern_ms / 1e6, 1) if traffic else None),
                          "traffic_frac": (round(traffic / kern_ms / 1e6 / peak, 4)
                                           if traffic else None)},
-            "gpu_launches": args.steps * (2 if eb else 1),
+            # per step: eb = merge path + product; rb with a workspace = the
+            # long-row list + long-row CTAs + row-block kernel; rb = product
+            "gpu_launches": args.steps * (2 if eb else (3 if ws_need else 1)),
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks, "schedules": schedules,
             "power_law_10m": variant,
             "vendor": vendor, "batched": batched, "served": served,

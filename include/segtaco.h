@@ -68,9 +68,9 @@ extern "C" {
 #define SEGTACO_FLAG_FLAT_WALK 32u /* walk each unit in batches of 32 nonzeros
                                       across rows (the default for eb_sr with
                                       16-byte vectors)                           */
-#define SEGTACO_FLAG_NO_LONG_ROWS 64u /* rb_sr: walk every row in the row-block
-                                         kernel, also the long ones (see
-                                         items_per_unit)                          */
+#define SEGTACO_FLAG_NO_LONG_ROWS 64u /* rb schedules: walk every row in the
+                                         row-block kernel, also the long ones
+                                         (see items_per_unit)                     */
 
 /* Tuning knobs.  Zero in a field means "choose automatically". */
 typedef struct segtaco_config {
@@ -82,11 +82,12 @@ typedef struct segtaco_config {
                              N, ldb and the pointers allow                     */
   int32_t rows_per_unit;  /* rb: rows handled by one lane group / warp            */
   int32_t items_per_unit; /* eb: merge-path items (rows + nonzeros) per unit.
-                             rb_sr with nnz >= 1M: rows of at least this many
+                             rb with nnz >= 1M: rows of at least this many
                              nonzeros (0 = 2048) go to long-row CTAs that stage B
-                             rows in shared memory for the whole CTA, each
-                             column still summed in storage order; the
-                             row-block kernel runs beside them on the others */
+                             rows in shared memory for the whole CTA (rb_sr:
+                             each column still summed in storage order; rb_pr:
+                             four warps' partial sums folded); the row-block
+                             kernel runs beside them on the other rows        */
   uint32_t flags;         /* SEGTACO_FLAG_*                                        */
   int32_t depth;          /* row walk: dense loads in flight per lane (0 = 4, 4, 8) */
 } segtaco_config;
@@ -120,9 +121,9 @@ int segtaco_spmm(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr, cons
  * owns the device memory, a serving loop with a memory budget fixed at
  * start-up, a caller that cannot take an allocation's device-wide sync -- the
  * element-balanced schedules' scratch (merge-path chunk coordinates) and
- * rb_sr's list of long rows come from a fixed 2 MiB array in the library's
- * device memory instead of a workspace (an rb_sr list of more than 262,143
- * rows is not made: every row then stays in the row-block kernel).  Limit: at most 262,143 merge-path chunks, i.e.
+ * the row-block schedules' list of long rows come from a fixed 2 MiB array in
+ * the library's device memory instead of a workspace (a list of more than
+ * 262,143 entries is not made: every row then stays in the row-block kernel).  Limit: at most 262,143 merge-path chunks, i.e.
  * ceil((M + nnz) / items_per_unit) <= 262,143 (M + nnz <= ~134M at the default
  * 512 items); larger problems get SEGTACO_EINVAL.  The first call on each
  * device looks up the array's address (cudaGetSymbolAddress) and should come
@@ -138,9 +139,9 @@ int segtaco_spmm_noalloc(int32_t M, int32_t K, int64_t nnz, const int32_t *row_p
  * the zeroing of the C rows that straddle chunk edges.  A following
  * segtaco_spmm with SEGTACO_FLAG_PARTITION_READY, the same config, workspace,
  * A, C and N runs only the product kernel.  Must be repeated before every
- * product (the zeroing belongs to one product).  For rb_sr with long-row
- * CTAs (see items_per_unit) it lists the long rows instead; no-op for the
- * other rb cases.  workspace must be the caller's (not NULL). */
+ * product (the zeroing belongs to one product).  For rb schedules with
+ * long-row CTAs (see items_per_unit) it lists the long rows instead; no-op
+ * for the other rb cases.  workspace must be the caller's (not NULL). */
 int segtaco_spmm_partition(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr,
                            float *C, int64_t ldc, int32_t N, int32_t b_dtype,
                            const segtaco_config *cfg, void *workspace, size_t workspace_bytes,

@@ -62,7 +62,7 @@ void *Scratch::take(size_t bytes) {
 // ---------------------------------------------------------------------------
 static bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
 
-// rb_sr products below this many nonzeros walk every row in the row-block
+// Row-block products below this many nonzeros walk every row in the row-block
 // kernel: the list pass and the fork would cost more than a long row there.
 constexpr long long kLongRowsMinNnz = 1000000;
 // Default long-row threshold.  Measured on GB300 (1M x 1M power law, N = 128,
@@ -160,8 +160,8 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
     plan->items_per_unit = D;
     plan->nchunks = nch;
     plan->px_entries = plan->py_entries = nch + 1;
-  } else if (schedule == SEGTACO_RB_SR && nnz >= kLongRowsMinNnz &&
-             !(c.flags & SEGTACO_FLAG_NO_LONG_ROWS) && plan->walk != 2 && !plan->use_tma) {
+  } else if (nnz >= kLongRowsMinNnz && !(c.flags & SEGTACO_FLAG_NO_LONG_ROWS) &&
+             plan->walk != 2 && !plan->use_tma) {
     // Long rows to CTAs of their own (spmm_long.cu): their ring copies 16-byte
     // chunks of B rows, so B, ldb and N must allow 16-byte pieces.
     const int epc = 16 / esz;
@@ -311,8 +311,9 @@ int segtaco_autotune_heuristic(int32_t M, int32_t K, int64_t nnz, int32_t N, int
   // with B in L2 (banded, N = 64) 8 stays faster (0.224 vs 0.235 ms).
   if (!sequential && esz == 2 && bbytes > 48e6 && N % 16 == 0 && (skewed || nnz >= 4000000))
     cfg->vec = 16;
-  // eb: merge-path items per chunk; rb_sr: the long-row threshold.
-  cfg->items_per_unit = schedule == SEGTACO_RB_SR ? (int)kLongRowDefault : 512;
+  // eb: merge-path items per chunk; rb: the long-row threshold.
+  cfg->items_per_unit =
+      (schedule == SEGTACO_RB_SR || schedule == SEGTACO_RB_PR) ? (int)kLongRowDefault : 512;
   cfg->rows_per_unit = schedule == SEGTACO_RB_PR || schedule == SEGTACO_RB_SR ? 4 : 1;
   cfg->depth = (schedule == SEGTACO_RB_SR || schedule == SEGTACO_RB_PR) ? 8 : 4;
   cfg->flags = 0;

@@ -75,7 +75,7 @@ struct SpmmLaunch {
   bool bulk_copies;            // ... with cp.async.bulk (TMA) rather than cp.async
   bool deep;                   // row walk: 8 sixteen-byte loads in flight per lane
   int walk;                    // kWalkRows / kWalkRowsDeep / kWalkFlat (spmm_kernels.cuh)
-  int long_row = 0;            // rb_sr: rows of >= long_row nonzeros go to spmm_long.cu
+  int long_row = 0;            // rb: rows of >= long_row nonzeros go to spmm_long.cu
 };
 // One launcher per (dense type, unit kind); each switches over (V, G).
 int launch_spmm_f32_rows(const SpmmLaunch &L, cudaStream_t s);
@@ -99,9 +99,9 @@ struct SpmmPlan {
   bool bulk_copies;
   bool deep;
   int walk;                  // kWalkRows / kWalkRowsDeep / kWalkFlat
-  int long_row;              // rb_sr: long-row threshold (0: every row in the row-block kernel)
+  int long_row;              // rb: long-row threshold (0: every row in the row-block kernel)
   long long px_entries;      // int32 entries of the first workspace array (eb: chunk-edge
-                             // rows; rb_sr long rows: the list of long rows)
+                             // rows; rb long rows: the list of long rows)
   long long py_entries;      // ... of the second (eb: chunk-edge nonzeros; long rows: counters)
   size_t workspace;          // bytes
 };
@@ -145,7 +145,7 @@ int launch_sddmm(int M, long long nnz, const int *row_ptr, const int *col, const
                  const void *X, const void *Y, int x_dtype, long long ldx, long long ldy, int D,
                  float *out, int *starts, int P, long long nblk, cudaStream_t s,
                  bool starts_ready = false);
-// ---- rb_sr long rows (spmm_long.cu) ----
+// ---- long rows of the row-block schedules (spmm_long.cu) ----
 // The two parts of the long-row list for threshold T: rows of >= 8T nonzeros
 // (at most nnz / 8T of them) and rows of T .. 8T-1 (at most nnz / T).
 inline void long_list_caps(long long nnz, long long T, long long *hi, long long *lo) {

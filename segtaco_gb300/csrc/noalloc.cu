@@ -76,7 +76,7 @@ extern "C" int segtaco_spmm_noalloc(int32_t M, int32_t K, int64_t nnz, const int
   SpmmPlan plan;
   SEGTACO_TRY(plan_spmm(M, K, nnz, N, b_dtype, ldb, ldc, B, C, cfg, &plan));
   if (plan.long_row > 0 && plan.px_entries > kNoallocEntries) {
-    // the rb_sr long-row list would not fit: every row in the row-block kernel
+    // the long-row list would not fit: every row in the row-block kernel
     plan.long_row = 0;
     plan.px_entries = plan.py_entries = 0;
     plan.workspace = 0;

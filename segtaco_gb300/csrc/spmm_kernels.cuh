@@ -61,8 +61,8 @@ template <typename BT> struct SpmmArgs {
   long long units;                 // number of warps' units (chunks or row blocks)
   int rows_per_unit;               // rb: rows per warp
   int l2_hints;                    // 1: gathered B rows evict_last in L2
-  int long_row;                    // rb_sr: rows of >= long_row nonzeros are left to
-                                   // the long-row CTAs (spmm_long.cu); 0: none
+  int long_row;                    // rb: rows of >= long_row nonzeros are left to the
+                                   // long-row CTAs (spmm_long.cu); 0: none
 };
 
 template <int V> __device__ __forceinline__ void zero(float (&a)[V]) {
@@ -141,7 +141,7 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
       rw = (wb + lane < M) ? __ldg(a.row_ptr + wb + 1 + lane) : INT_MAX;
     }
     const int rend = min(__shfl_sync(FULL, rw, cur - wb), y1);
-    if constexpr (P == 1 && ROWS) {
+    if constexpr (ROWS) {
       if (a.long_row > 0 && rend - cstart >= a.long_row) {
         // a long row: summed by the long-row CTAs; the batch buffer moves on
         cstart = rend;

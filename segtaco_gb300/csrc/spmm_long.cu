@@ -1,4 +1,4 @@
-// spmm_long.cu -- the long rows of a row-balanced sequential SpMM (rb_sr).
+// spmm_long.cu -- the long rows of the row-balanced SpMM schedules (rb_sr, rb_pr).
 //
 // In rb_sr every column of a row is one fmaf chain in storage order
 // (segTACO spmm_rb_sr.h:187-243: one thread sums a row serially), so the
@@ -28,6 +28,10 @@
 // Slabs of 32 columns (4 CTAs per row of N = 128, 7 x 64 rows in flight)
 // took 2.79 ms: the gathers of B (512 MB, beyond L2) make this kernel
 // DRAM-bound, and narrower slabs only re-read the row's indices.
+//
+// rb_pr splits a row over the lanes of one warp (segTACO spmm_rb_pr.h:223-375)
+// and meets the same tail; its long rows take the same CTAs, each warp
+// summing a quarter of every stage and the four partials folded at the end.
 #include <algorithm>
 #include <atomic>
 
@@ -67,6 +71,31 @@ template <int N> __device__ __forceinline__ void cp_async_wait() {
 __device__ __forceinline__ float to_f32(float x) { return x; }
 __device__ __forceinline__ float to_f32(uint16_t x) { return bf16lo(x); }
 
+// CPL consecutive dense values of a ring row as floats, in one shared load.
+template <typename BT, int CPL>
+__device__ __forceinline__ void lds_cols(const BT *p, float (&o)[CPL]) {
+  constexpr int BYTES = CPL * (int)sizeof(BT);
+  uint32_t w[BYTES >= 4 ? BYTES / 4 : 1];
+  if constexpr (BYTES == 16) {
+    const uint4 x = *reinterpret_cast<const uint4 *>(p);
+    w[0] = x.x, w[1] = x.y, w[2] = x.z, w[3] = x.w;
+  } else if constexpr (BYTES == 8) {
+    const uint2 x = *reinterpret_cast<const uint2 *>(p);
+    w[0] = x.x, w[1] = x.y;
+  } else if constexpr (BYTES == 4) {
+    w[0] = *reinterpret_cast<const uint32_t *>(p);
+  } else {
+    w[0] = *reinterpret_cast<const uint16_t *>(p);
+  }
+#pragma unroll
+  for (int v = 0; v < CPL; ++v) {
+    if constexpr (sizeof(BT) == 4)
+      o[v] = __uint_as_float(w[v]);
+    else
+      o[v] = (v & 1) ? bf16hi(w[v >> 1]) : bf16lo(w[v >> 1]);
+  }
+}
+
 __global__ void long_rows_list_kernel(const int *__restrict__ row_ptr, int M, int long_row,
                                       int *__restrict__ list, long long cap_hi,
                                       long long cap_lo, int *counters) {
@@ -83,10 +112,14 @@ __global__ void long_rows_list_kernel(const int *__restrict__ row_ptr, int M, in
   }
 }
 
-// One CTA per (column slab of W columns, long row) item at a time.  Thread t
-// sums column slab*W + t (t < W); every thread copies: a row segment is
-// CH = W / EPC sixteen-byte chunks, RP = 128 / CH rows per pass of the CTA.
-template <typename BT, int W>
+// One CTA per (column slab of W columns, long row) item at a time; every
+// thread copies: a row segment is CH = W / EPC sixteen-byte chunks, RP = 128 /
+// CH rows per pass of the CTA.  Sequential (rb_sr): thread t sums column
+// slab*W + t (t < W) over the whole row in storage order.  Parallel (PR,
+// rb_pr): warp w sums rows w*16 .. w*16+15 of every stage of 64, lane l
+// columns l*W/32 .. (l+1)*W/32-1 (one shared load), and the four warps'
+// partial sums are folded as (w0 + w1) + (w2 + w3) at the row's end.
+template <typename BT, int W, bool PR>
 __global__ void __launch_bounds__(kLongCta)
     spmm_long_rows_kernel(SpmmArgs<BT> a, const int *__restrict__ list, long long cap_hi,
                           long long cap_lo, int *counters, int slabs) {
@@ -163,7 +196,13 @@ __global__ void __launch_bounds__(kLongCta)
     }
     if (kLongRing - 1 < nst) load_cols(kLongRing - 1);
 
+    constexpr int CPL = W / 32;             // PR: columns per lane
+    constexpr int RW = kLongStage / 4;      // PR: rows of a stage per warp
+    const int warp = t >> 5, lane = t & 31;
     float acc = 0.0f;
+    float pacc[CPL];
+#pragma unroll
+    for (int v = 0; v < CPL; ++v) pacc[v] = 0.0f;
     for (int st = 0; st < nst; ++st) {
       cp_async_wait<kLongRing - 2>();  // stage st has landed (this thread's copies) ...
       __syncthreads();                 // ... and every thread's; slot st-1 is free
@@ -171,7 +210,21 @@ __global__ void __launch_bounds__(kLongCta)
       if (sn < nst) issue(sn);
       cp_async_commit();
       if (sn + 1 < nst) load_cols(sn + 1);
-      if (t < W) {
+      if constexpr (PR) {
+        const int slot = st % kLongRing;
+        const BT *src = ring + (size_t)slot * kLongStage * W + lane * CPL;
+        const float *vs = vring + slot * kLongStage;
+        const int cnt = min(kLongStage, pe - (pb + st * kLongStage));
+        const int iend = min(warp * RW + RW, cnt);
+#pragma unroll 4
+        for (int i = warp * RW; i < iend; ++i) {
+          float b[CPL];
+          lds_cols<BT, CPL>(src + i * W, b);
+          const float v = vs[i];
+#pragma unroll
+          for (int u = 0; u < CPL; ++u) pacc[u] = fmaf(v, b[u], pacc[u]);
+        }
+      } else if (t < W) {
         const int slot = st % kLongRing;
         const BT *src = ring + (size_t)slot * kLongStage * W + t;
         const float *vs = vring + slot * kLongStage;
@@ -184,6 +237,16 @@ __global__ void __launch_bounds__(kLongCta)
         }
       }
     }
+    if constexpr (PR) {
+      // Fold the warps' partial sums through the (drained) ring.
+      float *part = reinterpret_cast<float *>(smem);  // [4][W]
+      __syncthreads();
+#pragma unroll
+      for (int u = 0; u < CPL; ++u) part[warp * W + lane * CPL + u] = pacc[u];
+      __syncthreads();
+      if (t < W)
+        acc = (part[t] + part[W + t]) + (part[2 * W + t] + part[3 * W + t]);
+    }
     if (t < W && col0 + t < a.N) a.C[(long long)r * a.ldc + col0 + t] = acc;
   }
 }
@@ -192,7 +255,7 @@ template <typename BT, int W> constexpr size_t long_smem_bytes() {
   return sizeof(BT) * kLongRing * kLongStage * W + sizeof(float) * kLongRing * kLongStage;
 }
 
-template <typename BT, int W>
+template <typename BT, int W, bool PR>
 int launch_long_kernel(const SpmmArgs<BT> &a, const int *list, int *counters, int sms,
                        cudaStream_t s) {
   long long cap_hi, cap_lo;
@@ -205,7 +268,7 @@ int launch_long_kernel(const SpmmArgs<BT> &a, const int *list, int *counters, in
   SEGTACO_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
   const unsigned long long bit = 1ull << (dev & 63);
   if (!(opted.load() & bit)) {
-    SEGTACO_TRY(check_cuda(cudaFuncSetAttribute(spmm_long_rows_kernel<BT, W>,
+    SEGTACO_TRY(check_cuda(cudaFuncSetAttribute(spmm_long_rows_kernel<BT, W, PR>,
                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 (int)bytes),
                            "cudaFuncSetAttribute(spmm_long_rows_kernel)"));
@@ -216,7 +279,7 @@ int launch_long_kernel(const SpmmArgs<BT> &a, const int *list, int *counters, in
   // per SM and at most one per item.
   const long long per_sm = bytes <= 100 * 1024 ? 2 : 1;
   const long long g = std::min<long long>(sms * per_sm, (cap_hi + cap_lo) * (long long)slabs);
-  spmm_long_rows_kernel<BT, W><<<(unsigned)std::max<long long>(g, 1), kLongCta, bytes, s>>>(
+  spmm_long_rows_kernel<BT, W, PR><<<(unsigned)std::max<long long>(g, 1), kLongCta, bytes, s>>>(
       a, list, cap_hi, cap_lo, counters, slabs);
   return check_launch("spmm_long_rows_kernel");
 }
@@ -226,9 +289,15 @@ int launch_long_typed(const SpmmLaunch &L, const int *list, int *counters, int s
                       cudaStream_t s) {
   const SpmmArgs<BT> a = make_spmm_args<BT>(L);
   // Slabs of 128 columns (one per row at N <= 128); 32 or 64 for narrower N.
-  if (L.N <= 32) return launch_long_kernel<BT, 32>(a, list, counters, sms, s);
-  if (L.N <= 64) return launch_long_kernel<BT, 64>(a, list, counters, sms, s);
-  return launch_long_kernel<BT, 128>(a, list, counters, sms, s);
+  // rb_sr plans one slot of 32 lanes (G = 32), rb_pr several.
+  if (L.G == 32) {
+    if (L.N <= 32) return launch_long_kernel<BT, 32, false>(a, list, counters, sms, s);
+    if (L.N <= 64) return launch_long_kernel<BT, 64, false>(a, list, counters, sms, s);
+    return launch_long_kernel<BT, 128, false>(a, list, counters, sms, s);
+  }
+  if (L.N <= 32) return launch_long_kernel<BT, 32, true>(a, list, counters, sms, s);
+  if (L.N <= 64) return launch_long_kernel<BT, 64, true>(a, list, counters, sms, s);
+  return launch_long_kernel<BT, 128, true>(a, list, counters, sms, s);
 }
 
 // Side stream and events of one host thread on one device.  They are kept for

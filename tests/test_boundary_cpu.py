@@ -171,6 +171,9 @@ def test_workspace_and_heuristic(native_lib):
     assert ws(128, items_per_unit=512) == want(512)
     assert ws(128, flags=N.FLAG_NO_LONG_ROWS) == 0
     assert ws(126) == 0
+    c = N.Config.make(schedule="rb_pr")  # rb_pr: the same list
+    assert L.segtaco_spmm_workspace_size(10**6, 10**6, 2 * 10**7, 128, N.F32, C.byref(c),
+                                         C.byref(out)) == N.OK and out.value == want(2048)
     h = N.Config()
     h.schedule = -1
     assert L.segtaco_autotune_heuristic(16384, 16384, 262144, 32, N.F32, 16, C.byref(h)) == N.OK

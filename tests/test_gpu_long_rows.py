@@ -1,17 +1,19 @@
-"""rb_sr's long rows.  From 1M nonzeros on, rows of at least items_per_unit
-(default 2048) nonzeros are summed by CTAs of their own that stage B row
-segments in shared memory, beside the row-block kernel on a forked stream.
-Every column stays one fmaf chain in storage order, so the result must be
-bit-identical to the one-warp walk (FLAG_NO_LONG_ROWS) and to the sequential
-FP32 FMA restatement of segTACO's serial row sum (spmm_rb_sr.h:187-243):
-across thresholds, widths (one and several column slabs, widths the 16-byte
-copies cannot take), bf16 B, unit values, offset B, the partition-ready
-split, and graph capture (the allocation-free entry point: test_zz_no_alloc.py)."""
+"""Long rows of the row-block schedules.  From 1M nonzeros on, rows of at
+least items_per_unit (default 2048) nonzeros are summed by CTAs of their own
+that stage B row segments in shared memory, beside the row-block kernel on a
+forked stream.  rb_sr: every column stays one fmaf chain in storage order, so
+the result must be bit-identical to the one-warp walk (FLAG_NO_LONG_ROWS) and
+to the sequential FP32 FMA restatement of segTACO's serial row sum
+(spmm_rb_sr.h:187-243): across thresholds, widths (one and several column
+slabs, widths the 16-byte copies cannot take), bf16 B, unit values, offset B,
+the partition-ready split, and graph capture (the allocation-free entry point:
+test_zz_no_alloc.py).  rb_pr: four warps' partial sums folded, within the
+FP64 bound of 1e-5 and bit-identical from run to run."""
 import numpy as np
 import pytest
 import torch
 
-from gpu_util import dev, to_torch_bf16
+from gpu_util import assert_spmm_close, dev, spmm_ref, to_torch_bf16
 from oracle import oracle as O
 from segtaco_gb300 import native as N
 from segtaco_gb300 import ops, synth
@@ -46,9 +48,9 @@ def rowseq(A, B, val=None):
     return O.spmm_f32_rowseq(A.row_ptr, A.col, A.val if val is None else val, B, fma=True)
 
 
-def run(Ad, Bd, n, **kw):
+def run(Ad, Bd, n, schedule="rb_sr", **kw):
     C_ = torch.full((Ad.M, n), float("nan"), device="cuda")
-    ops.spmm(Ad, Bd, C_out=C_, config=N.Config.make(schedule="rb_sr", **kw))
+    ops.spmm(Ad, Bd, C_out=C_, config=N.Config.make(schedule=schedule, **kw))
     torch.cuda.synchronize()
     return C_.cpu().numpy()
 
@@ -135,3 +137,24 @@ def test_graph_capture(cuda, A):
         torch.cuda.synchronize()
         assert np.array_equal(C_.cpu().numpy(), want)
 
+
+
+@pytest.mark.parametrize("n", [128, 96, 64, 32, 8, 200, 126])
+def test_rb_pr_long_rows(cuda, A, n):
+    B = synth.dense(A.K, n, seed=50 + n)
+    Ad, Bd = dev(A), torch.from_numpy(B).cuda()
+    ref = spmm_ref(A, B)
+    got = run(Ad, Bd, n, "rb_pr")
+    assert_spmm_close(got, A, B, ref=ref)
+    assert np.array_equal(got, run(Ad, Bd, n, "rb_pr"))  # no atomics: identical reruns
+    assert_spmm_close(run(Ad, Bd, n, "rb_pr", flags=N.FLAG_NO_LONG_ROWS), A, B, ref=ref)
+
+
+@pytest.mark.parametrize("threshold", [1, 512, 2_049])
+def test_rb_pr_thresholds_and_bf16(cuda, A, threshold):
+    bits = synth.to_bf16_bits(synth.dense(A.K, 64, seed=60))
+    got = run(dev(A), to_torch_bf16(bits), 64, "rb_pr", items_per_unit=threshold)
+    assert_spmm_close(got, A, bits, bf16=True)
+    B = synth.dense(A.K, 128, seed=61)
+    got = run(dev(A), torch.from_numpy(B).cuda(), 128, "rb_pr", items_per_unit=threshold)
+    assert_spmm_close(got, A, B)
