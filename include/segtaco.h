@@ -68,9 +68,11 @@ extern "C" {
 #define SEGTACO_FLAG_FLAT_WALK 32u /* walk each unit in batches of 32 nonzeros
                                       across rows (the default for eb_sr with
                                       16-byte vectors)                           */
-#define SEGTACO_FLAG_NO_LONG_ROWS 64u /* rb schedules: walk every row in the
-                                         row-block kernel, also the long ones
-                                         (see items_per_unit)                     */
+#define SEGTACO_FLAG_LONG_ROWS 64u /* rb schedules with nnz >= 1M: rows of at
+                                      least items_per_unit nonzeros go to
+                                      long-row CTAs (see items_per_unit);
+                                      segtaco_autotune_heuristic sets it when
+                                      the longest row reaches that length      */
 
 /* Tuning knobs.  Zero in a field means "choose automatically". */
 typedef struct segtaco_config {
@@ -82,12 +84,13 @@ typedef struct segtaco_config {
                              N, ldb and the pointers allow                     */
   int32_t rows_per_unit;  /* rb: rows handled by one lane group / warp            */
   int32_t items_per_unit; /* eb: merge-path items (rows + nonzeros) per unit.
-                             rb with nnz >= 1M: rows of at least this many
-                             nonzeros (0 = 2048) go to long-row CTAs that stage B
-                             rows in shared memory for the whole CTA (rb_sr:
-                             each column still summed in storage order; rb_pr:
-                             four warps' partial sums folded); the row-block
-                             kernel runs beside them on the other rows        */
+                             rb with SEGTACO_FLAG_LONG_ROWS and nnz >= 1M:
+                             rows of at least this many nonzeros (0 = 2048) go
+                             to long-row CTAs that stage B rows in shared
+                             memory for the whole CTA (rb_sr: each column
+                             still summed in storage order; rb_pr: four warps'
+                             partial sums folded); the row-block kernel runs
+                             beside them on the other rows                   */
   uint32_t flags;         /* SEGTACO_FLAG_*                                        */
   int32_t depth;          /* row walk: dense loads in flight per lane (0 = 4, 4, 8) */
 } segtaco_config;

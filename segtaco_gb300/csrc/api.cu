@@ -62,12 +62,6 @@ void *Scratch::take(size_t bytes) {
 // ---------------------------------------------------------------------------
 static bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
 
-// Row-block products below this many nonzeros walk every row in the row-block
-// kernel: the list pass and the fork would cost more than a long row there.
-constexpr long long kLongRowsMinNnz = 1000000;
-// Default long-row threshold.  Measured on GB300 (1M x 1M power law, N = 128,
-// Zipf 1.8 / 1.922): 1024: 2.33 / 1.45 ms, 2048: 2.27 / 1.44, 4096: 2.23 / 1.46.
-constexpr long long kLongRowDefault = 2048;
 
 int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, long long ldc,
               const void *B, const float *C, const segtaco_config *cfg, SpmmPlan *plan) {
@@ -160,13 +154,13 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
     plan->items_per_unit = D;
     plan->nchunks = nch;
     plan->px_entries = plan->py_entries = nch + 1;
-  } else if (nnz >= kLongRowsMinNnz && !(c.flags & SEGTACO_FLAG_NO_LONG_ROWS) &&
+  } else if (nnz >= kLongRowsMinNnz && (c.flags & SEGTACO_FLAG_LONG_ROWS) &&
              plan->walk != 2 && !plan->use_tma) {
     // Long rows to CTAs of their own (spmm_long.cu): their ring copies 16-byte
     // chunks of B rows, so B, ldb and N must allow 16-byte pieces.
     const int epc = 16 / esz;
     if (N % epc == 0 && ldb % epc == 0 && ((uintptr_t)B % 16) == 0) {
-      long long T = c.items_per_unit > 0 ? c.items_per_unit : kLongRowDefault;
+      long long T = long_row_threshold(c);
       if (T > nnz) T = nnz;
       long long hi, lo;
       long_list_caps(nnz, T, &hi, &lo);
@@ -290,11 +284,16 @@ int segtaco_autotune_heuristic(int32_t M, int32_t K, int64_t nnz, int32_t N, int
     cfg->col_tile = 32 * (16 / esz);
   else
     cfg->col_tile = bbytes <= 48e6 ? (N <= 64 * 4 / esz ? N : 64 * 4 / esz) : 128 / esz;
-  // rb_sr from 1M nonzeros hands its long rows to CTAs of their own
-  // (spmm_long.cu); its row-block kernel then takes 128-column slabs also for
+  // Row-block schedules from 1M nonzeros whose longest row reaches the
+  // long-row threshold hand those rows to CTAs of their own (spmm_long.cu;
+  // without row statistics they stay in the row-block kernel: the long-row
+  // launch costs its L1 carveout, banded 262,144 rows N = 64 rb_pr 0.344 ->
+  // 0.435 ms).  rb_sr's row-block kernel then takes 128-column slabs also for
   // bf16 (8-byte lanes).  Measured on GB300, 1M x 1M power law, N = 128:
   // fp32 2.32 ms (64-column slabs: 2.45), bf16 2.29 ms (256: 2.52).
-  if (schedule == SEGTACO_RB_SR && nnz >= 1000000) cfg->col_tile = 128;
+  const bool long_rows = (schedule == SEGTACO_RB_SR || schedule == SEGTACO_RB_PR) &&
+                         nnz >= kLongRowsMinNnz && max_row_len >= kLongRowDefault;
+  if (schedule == SEGTACO_RB_SR && long_rows) cfg->col_tile = 128;
   // fp32 with B beyond L2 (32-column slabs): 8 columns per lane (one 32-byte
   // load, 4 lanes per 128-byte segment, 8 slots), so a warp step covers 8 rows
   // or 8 nonzeros instead of 4.  Measured on GB300: 1M x 1M power law (skewed
@@ -316,7 +315,7 @@ int segtaco_autotune_heuristic(int32_t M, int32_t K, int64_t nnz, int32_t N, int
       (schedule == SEGTACO_RB_SR || schedule == SEGTACO_RB_PR) ? (int)kLongRowDefault : 512;
   cfg->rows_per_unit = schedule == SEGTACO_RB_PR || schedule == SEGTACO_RB_SR ? 4 : 1;
   cfg->depth = (schedule == SEGTACO_RB_SR || schedule == SEGTACO_RB_PR) ? 8 : 4;
-  cfg->flags = 0;
+  cfg->flags = long_rows ? SEGTACO_FLAG_LONG_ROWS : 0;
   return SEGTACO_OK;
 }
 

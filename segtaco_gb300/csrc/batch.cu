@@ -348,7 +348,7 @@ int plan_batch_problem(const segtaco_spmm_problem &p, const segtaco_config *cfg,
   c.depth = 0;
   c.flags &= ~(SEGTACO_FLAG_SMEM_RING | SEGTACO_FLAG_TMA_BULK | SEGTACO_FLAG_PARTITION_READY);
   // The persistent kernel walks every row of its items (no long-row CTAs).
-  c.flags |= SEGTACO_FLAG_NO_LONG_ROWS;
+  c.flags &= ~SEGTACO_FLAG_LONG_ROWS;
   *used = c;
   return plan_spmm(p.M, p.K, p.nnz, p.N, p.b_dtype, p.ldb, p.ldc, p.B, p.C, &c, plan);
 }

@@ -76,6 +76,7 @@ struct SpmmLaunch {
   bool deep;                   // row walk: 8 sixteen-byte loads in flight per lane
   int walk;                    // kWalkRows / kWalkRowsDeep / kWalkFlat (spmm_kernels.cuh)
   int long_row = 0;            // rb: rows of >= long_row nonzeros go to spmm_long.cu
+  int carveout = -1;           // >= 0: preferred shared-memory carveout (%) of the launch
 };
 // One launcher per (dense type, unit kind); each switches over (V, G).
 int launch_spmm_f32_rows(const SpmmLaunch &L, cudaStream_t s);
@@ -146,6 +147,16 @@ int launch_sddmm(int M, long long nnz, const int *row_ptr, const int *col, const
                  float *out, int *starts, int P, long long nblk, cudaStream_t s,
                  bool starts_ready = false);
 // ---- long rows of the row-block schedules (spmm_long.cu) ----
+// Row-block products below this many nonzeros walk every row in the row-block
+// kernel: the list pass and the fork would cost more than a long row there.
+constexpr long long kLongRowsMinNnz = 1000000;
+// Default long-row threshold (items_per_unit = 0).  Measured on GB300 (1M x 1M
+// power law, N = 128, Zipf 1.8 / 1.922, rb_sr): 1024: 2.33 / 1.45 ms, 2048:
+// 2.27 / 1.44, 4096: 2.23 / 1.46.
+constexpr long long kLongRowDefault = 2048;
+inline long long long_row_threshold(const segtaco_config &c) {
+  return c.items_per_unit > 0 ? c.items_per_unit : kLongRowDefault;
+}
 // The two parts of the long-row list for threshold T: rows of >= 8T nonzeros
 // (at most nnz / 8T of them) and rows of T .. 8T-1 (at most nnz / T).
 inline void long_list_caps(long long nnz, long long T, long long *hi, long long *lo) {

@@ -3,7 +3,7 @@
 
 #define SEGTACO_SPMM_CASE(V, G, R)                                   \
   case V * 100 + G:                                                  \
-    spmm_seg_kernel<uint16_t, V, G, R><<<grid, kSpmmCta, 0, s>>>(a);        \
+    launch_seg(spmm_seg_kernel<uint16_t, V, G, R>, grid, s, a, L.carveout);   \
     break;
 
 SEGTACO_DEFINE_SPMM_LAUNCHER(launch_spmm_bf16_rows, uint16_t, SEGTACO_VG_BF16, true)

@@ -3,7 +3,7 @@
 
 #define SEGTACO_SPMM_CASE(V, G, R)                                   \
   case V * 100 + G:                                                  \
-    spmm_seg_kernel<float, V, G, R><<<grid, kSpmmCta, 0, s>>>(a);        \
+    launch_seg(spmm_seg_kernel<float, V, G, R>, grid, s, a, L.carveout);   \
     break;
 
 SEGTACO_DEFINE_SPMM_LAUNCHER(launch_spmm_f32_chunks, float, SEGTACO_VG_F32, false)

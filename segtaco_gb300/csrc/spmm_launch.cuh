@@ -31,6 +31,29 @@ template <typename BT> inline SpmmArgs<BT> make_spmm_args(const SpmmLaunch &L) {
   return a;
 }
 
+// A launch of one SpMM kernel variant; carveout >= 0 asks for that percentage
+// of the SM's unified L1 / shared memory as shared memory for this launch
+// (the row-block kernel beside the long-row CTAs, spmm_long.cu).
+template <typename BT>
+inline void launch_seg(void (*kern)(SpmmArgs<BT>), dim3 grid, cudaStream_t s,
+                       const SpmmArgs<BT> &a, int carveout) {
+  if (carveout < 0) {
+    kern<<<grid, kSpmmCta, 0, s>>>(a);
+    return;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(kSpmmCta);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributePreferredSharedMemoryCarveout;
+  attr[0].val.sharedMemCarveout = (unsigned)carveout;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, a);  // errors surface in the caller's check_launch
+}
+
 // One warp per unit (x), one column slab per blockIdx.y.
 inline dim3 spmm_grid(const SpmmLaunch &L) {
   const long long W = (long long)L.V * L.G;
@@ -52,9 +75,9 @@ inline dim3 spmm_grid(const SpmmLaunch &L) {
 
 // Sixteen-byte-vector variants of the other walks: the row walk with 8 loads
 // in flight per lane (kWalkRowsDeep) and the flat walk (kWalkFlat).
-#define SEGTACO_WALK_CASE(BT, G, R, WALK) \
-  case G:                                 \
-    spmm_seg_kernel<BT, 16 / sizeof(BT), G, R, WALK><<<grid, kSpmmCta, 0, s>>>(a); \
+#define SEGTACO_WALK_CASE(BT, G, R, WALK)                                              \
+  case G:                                                                              \
+    launch_seg(spmm_seg_kernel<BT, 16 / sizeof(BT), G, R, WALK>, grid, s, a, L.carveout); \
     break;
 #define SEGTACO_WALK_CASES(BT, R, WALK)                                                 \
   SEGTACO_WALK_CASE(BT, 1, R, WALK) SEGTACO_WALK_CASE(BT, 2, R, WALK)                   \

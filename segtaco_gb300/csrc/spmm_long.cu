@@ -40,15 +40,17 @@
 namespace segtaco {
 namespace {
 
-#ifndef SEGTACO_LONG_STAGE
-#define SEGTACO_LONG_STAGE 64
-#endif
-#ifndef SEGTACO_LONG_RING
-#define SEGTACO_LONG_RING 4
-#endif
-constexpr int kLongCta = 128;                  // threads of a long-row CTA
-constexpr int kLongStage = SEGTACO_LONG_STAGE;  // nonzeros per ring stage
-constexpr int kLongRing = SEGTACO_LONG_RING;    // stages in the ring (all but one in flight)
+constexpr int kLongCta = 128;   // threads of a long-row CTA
+constexpr int kLongStage = 64;  // nonzeros per ring stage
+constexpr int kLongRing = 4;    // stages in the ring (all but one in flight)
+// The long-row CTAs launch at the device's highest priority and the row-block
+// kernel beside them asks for the whole unified L1 as shared memory (it uses
+// none): otherwise its CTAs fill the SMs first, under a carveout too small for
+// a 132 KB ring, and the long rows wait for its last wave.  Measured on GB300
+// (1M x 1M power law, N = 128, rb_sr / rb_pr): 2.01 / 2.11 ms without either,
+// 1.95 / 2.01 with the priority, 2.17 / 2.22 with the carveout, 1.69 / 1.70
+// with both (bf16 B: 1.25 / 1.36 -> 0.93 / 1.06).
+constexpr int kRowBlockCarveout = 100;
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -279,9 +281,22 @@ int launch_long_kernel(const SpmmArgs<BT> &a, const int *list, int *counters, in
   // per SM and at most one per item.
   const long long per_sm = bytes <= 100 * 1024 ? 2 : 1;
   const long long g = std::min<long long>(sms * per_sm, (cap_hi + cap_lo) * (long long)slabs);
-  spmm_long_rows_kernel<BT, W, PR><<<(unsigned)std::max<long long>(g, 1), kLongCta, bytes, s>>>(
-      a, list, cap_hi, cap_lo, counters, slabs);
-  return check_launch("spmm_long_rows_kernel");
+  int least = 0, greatest = 0;
+  SEGTACO_TRY(check_cuda(cudaDeviceGetStreamPriorityRange(&least, &greatest),
+                         "cudaDeviceGetStreamPriorityRange"));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)std::max<long long>(g, 1));
+  cfg.blockDim = dim3(kLongCta);
+  cfg.dynamicSmemBytes = bytes;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributePriority;
+  attr[0].val.priority = greatest;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return check_cuda(cudaLaunchKernelEx(&cfg, spmm_long_rows_kernel<BT, W, PR>, a, list, cap_hi,
+                                       cap_lo, counters, slabs),
+                    "cudaLaunchKernelEx(spmm_long_rows_kernel)");
 }
 
 template <typename BT>
@@ -367,20 +382,24 @@ int launch_long_rows_list(const int *row_ptr, int M, long long nnz, int long_row
 int launch_spmm_long_rows(const SpmmLaunch &L, const int *list, int *counters, cudaStream_t s) {
   const bool bf16 = L.dtype == SEGTACO_BF16;
   const int sms = sm_count();
+  // The work queue is cleared before the fork, so that the long-row kernel is
+  // the side stream's first operation and reaches the GPU before the
+  // row-block kernel.
+  SEGTACO_TRY(check_cuda(cudaMemsetAsync(counters + 2, 0, sizeof(unsigned long long), s),
+                         "cudaMemsetAsync"));
   LongFork *f = long_fork(s);
   cudaStream_t ls = f ? f->side : s;
   if (f) {
     SEGTACO_TRY(check_cuda(cudaEventRecord(f->start, s), "cudaEventRecord"));
     SEGTACO_TRY(check_cuda(cudaStreamWaitEvent(f->side, f->start, 0), "cudaStreamWaitEvent"));
   }
-  int st = check_cuda(cudaMemsetAsync(counters + 2, 0, sizeof(unsigned long long), ls),
-                      "cudaMemsetAsync");
-  if (st == SEGTACO_OK)
-    st = bf16 ? launch_long_typed<uint16_t>(L, list, counters, sms, ls)
-              : launch_long_typed<float>(L, list, counters, sms, ls);
+  int st = bf16 ? launch_long_typed<uint16_t>(L, list, counters, sms, ls)
+                : launch_long_typed<float>(L, list, counters, sms, ls);
   // The row-block kernel on the caller's stream (beside the side stream's
   // long-row CTAs when forked).
-  if (st == SEGTACO_OK) st = bf16 ? launch_spmm_bf16_rows(L, s) : launch_spmm_f32_rows(L, s);
+  SpmmLaunch R = L;
+  R.carveout = kRowBlockCarveout;
+  if (st == SEGTACO_OK) st = bf16 ? launch_spmm_bf16_rows(R, s) : launch_spmm_f32_rows(R, s);
   // Join the side stream whatever happened, so that a capture stays whole.
   if (f) {
     const int j1 = check_cuda(cudaEventRecord(f->done, f->side), "cudaEventRecord");

@@ -37,7 +37,7 @@ FLAG_SMEM_RING = 4
 FLAG_TMA_BULK = 8
 FLAG_ROW_WALK = 16
 FLAG_FLAT_WALK = 32
-FLAG_NO_LONG_ROWS = 64
+FLAG_LONG_ROWS = 64
 
 
 class SegtacoError(RuntimeError):

@@ -154,10 +154,10 @@ def test_workspace_and_heuristic(native_lib):
     assert L.segtaco_spmm_workspace_size(1000, 1000, 20000, 128, N.F32, C.byref(cfg),
                                          C.byref(out)) == N.OK
     assert out.value == 0
-    # rb_sr from 1M nonzeros: the list of rows of >= items_per_unit (2048)
-    # nonzeros in two parts (rows of >= 8 * 2048: at most nnz / 16384; the
-    # others: at most nnz / 2048) and the counters; none with NO_LONG_ROWS or
-    # when N is not a multiple of the 16-byte chunk
+    # rb with LONG_ROWS from 1M nonzeros: the list of rows of >= items_per_unit
+    # (2048) nonzeros in two parts (rows of >= 8 * 2048: at most nnz / 16384;
+    # the others: at most nnz / 2048) and the counters; none without the flag
+    # or when N is not a multiple of the 16-byte chunk
     def ws(n, **kw):
         c = N.Config.make(schedule="rb_sr", **kw)
         assert L.segtaco_spmm_workspace_size(10**6, 10**6, 2 * 10**7, n, N.F32, C.byref(c),
@@ -167,11 +167,12 @@ def test_workspace_and_heuristic(native_lib):
     def want(T):
         entries = 2 * 10**7 // (8 * T) + 1 + 2 * 10**7 // T + 1
         return (entries * 4 + 255) // 256 * 256 + 256
-    assert ws(128) == want(2048)
-    assert ws(128, items_per_unit=512) == want(512)
-    assert ws(128, flags=N.FLAG_NO_LONG_ROWS) == 0
-    assert ws(126) == 0
-    c = N.Config.make(schedule="rb_pr")  # rb_pr: the same list
+    LR = N.FLAG_LONG_ROWS
+    assert ws(128, flags=LR) == want(2048)
+    assert ws(128, items_per_unit=512, flags=LR) == want(512)
+    assert ws(128) == 0
+    assert ws(126, flags=LR) == 0
+    c = N.Config.make(schedule="rb_pr", flags=LR)  # rb_pr: the same list
     assert L.segtaco_spmm_workspace_size(10**6, 10**6, 2 * 10**7, 128, N.F32, C.byref(c),
                                          C.byref(out)) == N.OK and out.value == want(2048)
     h = N.Config()
@@ -195,12 +196,18 @@ def test_workspace_and_heuristic(native_lib):
     assert L.segtaco_autotune_heuristic(10**6, 10**6, 2 * 10**7, 128, N.BF16, 48679,
                                         C.byref(h)) == N.OK
     assert (h.col_tile, h.vec) == (64, 16)  # bf16 B beyond L2, skewed: 16 columns per lane
-    for sched, tile, items in ((N.RB_SR, 128, 2048), (N.EB_SR, 128, 512)):
-        h.schedule = sched  # sequential: 16-byte lanes; rb_sr: long-row threshold 2048
+    for sched, tile, items, flags in ((N.RB_SR, 128, 2048, N.FLAG_LONG_ROWS),
+                                      (N.EB_SR, 128, 512, 0)):
+        h.schedule = sched  # sequential: 16-byte lanes; rb_sr: long rows from 2048
         assert L.segtaco_autotune_heuristic(10**6, 10**6, 2 * 10**7, 128, N.F32, 48679,
                                             C.byref(h)) == N.OK
         assert h.schedule == sched and h.col_tile == tile and h.vec == 0
-        assert h.items_per_unit == items
+        assert h.items_per_unit == items and h.flags == flags
+    for max_len, flags in ((2047, 0), (2048, N.FLAG_LONG_ROWS), (-1, 0)):  # rows known short
+        h.schedule = N.RB_PR                                             # or unknown: none
+        assert L.segtaco_autotune_heuristic(10**6, 10**6, 2 * 10**7, 128, N.F32, max_len,
+                                            C.byref(h)) == N.OK
+        assert h.flags == flags
     h.schedule = N.RB_SR  # bf16 too: 128-column slabs (8-byte lanes) from 1M nonzeros
     assert L.segtaco_autotune_heuristic(10**6, 10**6, 2 * 10**7, 128, N.BF16, 48679,
                                         C.byref(h)) == N.OK

@@ -1,9 +1,9 @@
 """Long rows of the row-block schedules.  From 1M nonzeros on, rows of at
 least items_per_unit (default 2048) nonzeros are summed by CTAs of their own
 that stage B row segments in shared memory, beside the row-block kernel on a
-forked stream.  rb_sr: every column stays one fmaf chain in storage order, so
-the result must be bit-identical to the one-warp walk (FLAG_NO_LONG_ROWS) and
-to the sequential FP32 FMA restatement of segTACO's serial row sum
+forked stream (FLAG_LONG_ROWS).  rb_sr: every column stays one fmaf chain in
+storage order, so the result must be bit-identical to the one-warp walk
+(without the flag) and to the sequential FP32 FMA restatement of segTACO's serial row sum
 (spmm_rb_sr.h:187-243): across thresholds, widths (one and several column
 slabs, widths the 16-byte copies cannot take), bf16 B, unit values, offset B,
 the partition-ready split, and graph capture (the allocation-free entry point:
@@ -48,7 +48,8 @@ def rowseq(A, B, val=None):
     return O.spmm_f32_rowseq(A.row_ptr, A.col, A.val if val is None else val, B, fma=True)
 
 
-def run(Ad, Bd, n, schedule="rb_sr", **kw):
+def run(Ad, Bd, n, schedule="rb_sr", long=True, **kw):
+    kw["flags"] = kw.get("flags", 0) | (N.FLAG_LONG_ROWS if long else 0)
     C_ = torch.full((Ad.M, n), float("nan"), device="cuda")
     ops.spmm(Ad, Bd, C_out=C_, config=N.Config.make(schedule=schedule, **kw))
     torch.cuda.synchronize()
@@ -60,7 +61,7 @@ def test_bit_identical_to_one_warp_walk(cuda, A, n):
     B = synth.dense(A.K, n, seed=n)
     Ad, Bd = dev(A), torch.from_numpy(B).cuda()
     got = run(Ad, Bd, n)
-    assert np.array_equal(got, run(Ad, Bd, n, flags=N.FLAG_NO_LONG_ROWS))
+    assert np.array_equal(got, run(Ad, Bd, n, long=False))
     assert np.array_equal(got, rowseq(A, B))
 
 
@@ -77,7 +78,7 @@ def test_bf16_dense_operand(cuda, A, n):
     Bf = (bits.astype(np.uint32) << 16).view(np.float32)  # the bf16 values, exactly
     Ad, Bd = dev(A), to_torch_bf16(bits)
     got = run(Ad, Bd, n)
-    assert np.array_equal(got, run(Ad, Bd, n, flags=N.FLAG_NO_LONG_ROWS))
+    assert np.array_equal(got, run(Ad, Bd, n, long=False))
     assert np.array_equal(got, rowseq(A, Bf))
 
 
@@ -100,13 +101,13 @@ def test_partition_ready_and_reruns(cuda, A):
     PARTITION_READY reuse the list (the work queue is cleared per launch)."""
     B = synth.dense(A.K, 128, seed=8)
     Ad, Bd = dev(A), torch.from_numpy(B).cuda()
-    cfg = N.Config.make(schedule="rb_sr")
+    cfg = N.Config.make(schedule="rb_sr", flags=N.FLAG_LONG_ROWS)
     ws = torch.empty(ops.spmm_workspace_size(Ad, 128, N.F32, cfg), dtype=torch.uint8,
                      device="cuda")
     assert ws.numel() > 0
     C_ = torch.full((A.M, 128), float("nan"), device="cuda")
     ops.spmm_partition(Ad, C_, cfg, ws)
-    ready = N.Config.make(schedule="rb_sr", flags=N.FLAG_PARTITION_READY)
+    ready = N.Config.make(schedule="rb_sr", flags=N.FLAG_LONG_ROWS | N.FLAG_PARTITION_READY)
     want = rowseq(A, B)
     for _ in range(3):
         C_.fill_(float("nan"))
@@ -119,7 +120,7 @@ def test_graph_capture(cuda, A):
     """The fork to the side stream inside a captured graph, replayed."""
     B = synth.dense(A.K, 128, seed=9)
     Ad, Bd = dev(A), torch.from_numpy(B).cuda()
-    cfg = N.Config.make(schedule="rb_sr")
+    cfg = N.Config.make(schedule="rb_sr", flags=N.FLAG_LONG_ROWS)
     ws = torch.empty(ops.spmm_workspace_size(Ad, 128, N.F32, cfg), dtype=torch.uint8,
                      device="cuda")
     C_ = torch.empty((A.M, 128), device="cuda")
@@ -147,7 +148,7 @@ def test_rb_pr_long_rows(cuda, A, n):
     got = run(Ad, Bd, n, "rb_pr")
     assert_spmm_close(got, A, B, ref=ref)
     assert np.array_equal(got, run(Ad, Bd, n, "rb_pr"))  # no atomics: identical reruns
-    assert_spmm_close(run(Ad, Bd, n, "rb_pr", flags=N.FLAG_NO_LONG_ROWS), A, B, ref=ref)
+    assert_spmm_close(run(Ad, Bd, n, "rb_pr", long=False), A, B, ref=ref)
 
 
 @pytest.mark.parametrize("threshold", [1, 512, 2_049])

@@ -67,7 +67,7 @@ def test_noalloc_rb_sr_long_rows(cuda):
     B = synth.dense(A.K, 128, seed=36)
     Ad, Bd = dev(A), torch.from_numpy(B).cuda()
     want = O.spmm_f32_rowseq(A.row_ptr, A.col, A.val, B, fma=True)
-    cfg = N.Config.make(schedule="rb_sr")
+    cfg = N.Config.make(schedule="rb_sr", flags=N.FLAG_LONG_ROWS)
     for _ in range(2):
         Cd = torch.full((A.M, 128), float("nan"), device="cuda")
         assert _noalloc(Ad, Bd, Cd, cfg) == N.OK, N.last_error()
