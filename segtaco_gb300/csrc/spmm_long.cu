@@ -315,14 +315,14 @@ int launch_long_typed(const SpmmLaunch &L, const int *list, int *counters, int s
   return launch_long_kernel<BT, 128, true>(a, list, counters, sms, s);
 }
 
-// Side stream and events of one host thread on one device.  They are kept for
-// the thread's lifetime (a thread that moves to another device gets new ones).
+// Side stream and events of one host thread on one device, kept for the
+// thread's lifetime.
 struct LongFork {
-  int device = -1;
   cudaStream_t side = nullptr;
   cudaEvent_t start = nullptr, done = nullptr;
 };
-thread_local LongFork t_fork;
+constexpr int kForkDevices = 64;
+thread_local LongFork t_forks[kForkDevices];
 
 // The fork of this thread on the current device, created on first use (not
 // while `s` is being captured: then the caller runs both kernels on `s`).
@@ -332,7 +332,9 @@ LongFork *long_fork(cudaStream_t s) {
     cudaGetLastError();
     return nullptr;
   }
-  if (t_fork.device == dev && t_fork.side) return &t_fork;
+  if (dev < 0 || dev >= kForkDevices) return nullptr;
+  LongFork &t_fork = t_forks[dev];
+  if (t_fork.side) return &t_fork;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
     cudaGetLastError();
@@ -340,7 +342,6 @@ LongFork *long_fork(cudaStream_t s) {
   }
   if (cs != cudaStreamCaptureStatusNone) return nullptr;
   LongFork f;
-  f.device = dev;
   if (cudaStreamCreateWithFlags(&f.side, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&f.start, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&f.done, cudaEventDisableTiming) != cudaSuccess) {
@@ -354,16 +355,21 @@ LongFork *long_fork(cudaStream_t s) {
 }
 
 int sm_count() {
-  static int counts[64] = {0};
+  static std::atomic<int> counts[kForkDevices];
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
-  if (!counts[dev]) {
-    int n = 0;
-    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1)
-      n = 148;
-    counts[dev] = n;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kForkDevices) {
+    cudaGetLastError();
+    return 148;
   }
-  return counts[dev];
+  int n = counts[dev].load(std::memory_order_relaxed);
+  if (n < 1) {
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) {
+      cudaGetLastError();
+      n = 148;
+    }
+    counts[dev].store(n, std::memory_order_relaxed);
+  }
+  return n;
 }
 
 }  // namespace
