@@ -70,7 +70,13 @@ extern "C" {
                                       16-byte vectors)                           */
 #define SEGTACO_FLAG_LONG_ROWS 64u /* rb schedules with nnz >= 1M: rows of at
                                       least items_per_unit nonzeros go to
-                                      long-row CTAs (see items_per_unit);
+                                      long-row CTAs (see items_per_unit) on a
+                                      side stream the library forks from the
+                                      call's stream and joins before returning
+                                      (created by the first such call on a
+                                      host thread and device; a call captured
+                                      into a graph before that runs both
+                                      kernels on the call's stream);
                                       segtaco_autotune_heuristic sets it when
                                       the longest row reaches that length      */
 
@@ -126,9 +132,10 @@ int segtaco_spmm(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr, cons
  * element-balanced schedules' scratch (merge-path chunk coordinates) and
  * the row-block schedules' list of long rows come from a fixed 2 MiB array in
  * the library's device memory instead of a workspace (a list of more than
- * 262,143 entries is not made: every row then stays in the row-block kernel).  Limit: at most 262,143 merge-path chunks, i.e.
- * ceil((M + nnz) / items_per_unit) <= 262,143 (M + nnz <= ~134M at the default
- * 512 items); larger problems get SEGTACO_EINVAL.  The first call on each
+ * 262,143 entries is not made: every row then stays in the row-block kernel).
+ * Limit: at most 262,143 merge-path chunks, i.e. ceil((M + nnz) /
+ * items_per_unit) <= 262,143 (M + nnz <= ~134M at the default 512 items);
+ * larger problems get SEGTACO_EINVAL.  The first call on each
  * device looks up the array's address (cudaGetSymbolAddress) and should come
  * before any stream capture.  All calls share the array: calls that overlap on
  * the GPU race on it.  SEGTACO_FLAG_PARTITION_READY is not accepted. */
