@@ -207,6 +207,24 @@ def row_stats(A: DeviceCSR, stream=None):
     return tuple(out)
 
 
+def autotune(A, n: int, b_dtype=N.F32, schedule=N.AUTO, max_row_len: int | None = None):
+    """The library's configuration for C = A @ B with n columns
+    (segtaco_autotune_heuristic): the schedule (AUTO: row-balanced for even
+    rows, merge path otherwise), slab, lanes, units and, for row-balanced
+    schedules with rows of >= 2048 nonzeros from 1M nonzeros on, the long-row
+    CTAs.  `A` is a DeviceCSR (its longest row from segtaco_row_stats on the
+    device) or a host CSR (from its row_ptr), unless max_row_len is given."""
+    if max_row_len is None:
+        if isinstance(A, DeviceCSR):
+            max_row_len = int(row_stats(A)[0])
+        else:
+            max_row_len = int(np.diff(A.row_ptr).max()) if A.M > 0 else 0
+    cfg = N.Config.make(schedule=schedule)
+    N.check(N.lib().segtaco_autotune_heuristic(A.M, A.K, A.nnz, n, b_dtype, max_row_len,
+                                               C.byref(cfg)))
+    return cfg
+
+
 class Batch:
     """Many SpMMs planned together and run by one persistent launch per kernel
     variant (segtaco_batch_*).  `items` is a list of (DeviceCSR, B, C) with B

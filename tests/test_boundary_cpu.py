@@ -214,6 +214,21 @@ def test_workspace_and_heuristic(native_lib):
     assert h.col_tile == 128
 
 
+def test_autotune_from_a_host_csr(native_lib):
+    """ops.autotune on a host CSR: the longest row from its row_ptr."""
+    from segtaco_gb300 import ops, synth
+    A = synth.power_law(60_000, 50_000, 1.8, 40_000, 0.02, seed=35)  # 1.09M nonzeros
+    assert A.nnz >= 10**6 and A.row_lengths().max() >= 2048
+    c = ops.autotune(A, 128)
+    assert c.schedule == N.EB_PR and c.flags == 0  # skewed: merge path
+    c = ops.autotune(A, 128, schedule=N.RB_SR)
+    assert c.schedule == N.RB_SR and c.flags == N.FLAG_LONG_ROWS and c.items_per_unit == 2048
+    c = ops.autotune(A, 128, schedule=N.RB_PR, max_row_len=100)
+    assert c.flags == 0  # rows known to be short: every row in the row-block kernel
+    U = synth.uniform_rows(seed=0)
+    assert ops.autotune(U, 32).schedule == N.RB_PR  # even rows: row-balanced
+
+
 def test_flag_constants_match_the_header():
     """Every SEGTACO_FLAG_* of include/segtaco.h has the same value in native.py."""
     text = open(os.path.join(ROOT, "include", "segtaco.h")).read()
