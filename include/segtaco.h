@@ -137,8 +137,12 @@ int segtaco_spmm(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr, cons
  * items_per_unit) <= 262,143 (M + nnz <= ~134M at the default 512 items);
  * larger problems get SEGTACO_EINVAL.  The first call on each
  * device looks up the array's address (cudaGetSymbolAddress) and should come
- * before any stream capture.  All calls share the array: calls that overlap on
- * the GPU race on it.  SEGTACO_FLAG_PARTITION_READY is not accepted. */
+ * before any stream capture; the address is kept for the process, so a
+ * cudaDeviceReset of a device that served this call is not supported.  With
+ * SEGTACO_FLAG_LONG_ROWS the long-row CTAs run on `stream` itself (no side
+ * stream or events are created).  All calls share the array: calls that
+ * overlap on the GPU race on it.  SEGTACO_FLAG_PARTITION_READY is not
+ * accepted. */
 int segtaco_spmm_noalloc(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr,
                          const int32_t *col, const float *vals, const void *B, int32_t b_dtype,
                          int64_t ldb, float *C, int64_t ldc, int32_t N,

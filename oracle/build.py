@@ -58,6 +58,40 @@ def reference_tree_present() -> bool:
     return os.path.isfile(os.path.join(REFERENCE_TREE, "gpu_library.h"))
 
 
+# The one source fix the SpMSpV experiment header needs to compile against the
+# current taco_tensor_t (int32_t*** indices, float* vals): its driver builds the
+# sparse x with uint8_t pointers (matrix_experiments/spmspv_csr_gpu.h:54-58).
+# Only those allocations are retyped; spmspv_csr_cpu_taco_ref (:9-32), the CPU
+# reference the fixtures come from, is compiled as written.
+SPMSPV_HEADER = os.path.join("matrix_experiments", "spmspv_csr_gpu.h")
+SPMSPV_CAST_FIX = (
+    ("x_taco.indices = new uint8_t**[1*4];", "x_taco.indices = new int32_t**[1*4];"),
+    ("x_taco.indices[0] = new uint8_t*[2*4];", "x_taco.indices[0] = new int32_t*[2*4];"),
+    ("x_taco.indices[0][0] = (uint8_t*)malloc", "x_taco.indices[0][0] = (int32_t*)malloc"),
+    ("x_taco.indices[0][1] = (uint8_t*)malloc", "x_taco.indices[0][1] = (int32_t*)malloc"),
+    ("x_taco.vals = (uint8_t*)malloc", "x_taco.vals = (float*)malloc"),
+)
+PATCHED = os.path.join(REF_OUT, "patched")
+
+
+def _patched_spmspv_header() -> str:
+    """Scratch copy of the SpMSpV experiment header with SPMSPV_CAST_FIX applied
+    (written under the git-ignored oracle/_ref/patched, which precedes the
+    reference tree on the include path)."""
+    src = os.path.join(REFERENCE_TREE, SPMSPV_HEADER)
+    dst = os.path.join(PATCHED, SPMSPV_HEADER)
+    text = open(src).read()
+    for old, new in SPMSPV_CAST_FIX:
+        if text.count(old) != 1:
+            raise RuntimeError("SpMSpV cast fix does not apply: %r" % old)
+        text = text.replace(old, new)
+    os.makedirs(os.path.dirname(dst), exist_ok=True)
+    if not os.path.exists(dst) or open(dst).read() != text:
+        with open(dst, "w") as f:
+            f.write(text)
+    return dst
+
+
 def build_ref(force: bool = False) -> dict:
     """Compile the reference's own CPU code into oracle/_ref (x86 container only)."""
     if not reference_tree_present():
@@ -66,12 +100,13 @@ def build_ref(force: bool = False) -> dict:
     out = {}
     golden_src = os.path.join(HERE, "ref", "ref_golden.cpp")
     golden_bin = os.path.join(REF_OUT, "ref_golden")
-    if force or _stale(golden_bin, [golden_src, __file__]):
+    patched = _patched_spmspv_header()
+    if force or _stale(golden_bin, [golden_src, __file__, patched]):
         # The experiment drivers reference the GPU entry points, which are never
         # called here, hence the unresolved-symbol link option.  -ffp-contract=off keeps Eigen's
         # multiply and add separate, as on a host without FMA.
         _run(["g++", "-O2", "-std=c++14", "-fopenmp", "-w",
-              "-ffp-contract=off", "-DNDEBUG",
+              "-ffp-contract=off", "-DNDEBUG", "-I", PATCHED,
               "-I", REFERENCE_TREE, "-I", os.path.join(REFERENCE_TREE, "eigen-3.4.0"),
               "-I", "/usr/local/cuda/include",
               golden_src, "-o", golden_bin,

@@ -7,17 +7,20 @@
 //   ds.h                                   to_eigen_csr (:380-397), read_mtx_file (:183-268)
 //   matrix_experiments/spmm_csr_gpu.h      spmm_cpu_naive (:110-127)
 //   matrix_experiments/sddmm_csr_gpu.h     sddmm_csr_cpu_taco_ref (:9-50)
+//   matrix_experiments/spmspv_csr_gpu.h    spmspv_csr_cpu_taco_ref (:9-32)
 // and Eigen 3.4.0's sparse x dense product (SparseDenseProduct.h:109-146) is
 // reached through EigenCSR * EigenRowMajor exactly as typedef'd at ds.h:32-33.
 //
 // The experiment headers also define GPU drivers that call the kernel entry
 // points; those drivers are never executed here, so the link leaves the kernel
-// symbols unresolved (see oracle/build.py) and the SDDMM GPU names that
-// gpu_kernels.cuh comments out get empty stand-ins below.
+// symbols unresolved (see oracle/build.py) and the SDDMM / SpMSpV GPU names
+// that gpu_kernels.cuh comments out get empty stand-ins below.
 //
 // matrix_experiments/spmspv_csr_gpu.h does not compile against the current
-// taco_tensor_t (it assigns uint8_t*** to int32_t*** at :54-58), so its CPU
-// reference cannot be built unchanged; SpMSpV parity rests on the restatement.
+// taco_tensor_t as written (its driver assigns uint8_t*** to int32_t*** at
+// :54-58); oracle/build.py compiles a scratch copy in which only those
+// allocations are retyped (SPMSPV_CAST_FIX), so spmspv_csr_cpu_taco_ref itself
+// is segTACO's code unchanged.
 //
 // Protocol: ref_golden <mode> <in.bin> <out.bin>, raw little-endian arrays.
 //   mode "csr"   : in = i64 M,K,nnz ; i32 rows[nnz], cols[nnz] ; f32 vals[nnz]
@@ -27,6 +30,9 @@
 //   mode "spmv"  : in = i64 M,K,nnz ; i32 row_ptr, col ; f32 vals, x[K]    out = f32 y[M]
 //   mode "sddmm" : in = i64 M,K,D,nnz ; i32 row_ptr, col ; f64 vals, X[M*D], Y[K*D]
 //                  out = f64 out[nnz]
+//   mode "spmspv": in = i64 M,K,nnz,nx ; i32 col_ptr[K+1], row_idx[nnz] ; f64 vals[nnz] ;
+//                  i32 x_idx[nx] ; f64 x_vals[nx]       out = f64 y[M]
+//                  (A as CSC = the CSR of A^T, spmspv_csr_gpu.h:37-43)
 //   mode "mtx"   : in = path of a .mtx file (text)                         (read_mtx_file)
 //                  out = i64 nrow,ncol,nnz ; i32 indptr[nrow+1], indices[nnz]
 #include "ds.h"
@@ -34,10 +40,12 @@
 
 void sddmm_csr_gpu_taco(taco_tensor_t *, taco_tensor_t *, taco_tensor_t *, taco_tensor_t *) {}
 void sddmm_csr_gpu_warp(taco_tensor_t *, taco_tensor_t *, taco_tensor_t *, taco_tensor_t *) {}
+void spmspv_csr_gpu_taco(taco_tensor_t *, taco_tensor_t *, taco_tensor_t *) {}
 float get_gpu_timer_result() { return -1.0f; }
 
 #include "matrix_experiments/spmm_csr_gpu.h"
 #include "matrix_experiments/sddmm_csr_gpu.h"
+#include "matrix_experiments/spmspv_csr_gpu.h"
 
 Timer timer;
 std::ofstream log_file;
@@ -163,6 +171,29 @@ int main(int argc, char **argv) {
     taco_tensor_t tD = dense_view(K, D, Y.data());
     sddmm_csr_cpu_taco_ref(&tOut, &tB, &tC, &tD);
     wr(fo, out.data(), nnz);
+  } else if (mode == "spmspv") {
+    auto h = rd<int64_t>(fi, 4);
+    int M = (int)h[0], K = (int)h[1], nx = (int)h[3];
+    int64_t nnz = h[2];
+    auto cptr = rd<int32_t>(fi, K + 1);
+    auto ridx = rd<int32_t>(fi, nnz);
+    auto val = rd<double>(fi, nnz);
+    auto xi = rd<int32_t>(fi, nx);
+    auto xv = rd<double>(fi, nx);
+    std::vector<double> y(M, -1.0);
+    // spmspv_csr_cpu_taco_ref(y, A, x) reads A as CSC (indices[1]: col_ptr,
+    // row_idx), x as a sparse vector (indices[0]: pos {0, nx}, crd) and every
+    // value array as double.
+    taco_tensor_t tA = csr_view(K, M, cptr.data(), ridx.data(), val.data());
+    int32_t xpos[2] = {0, nx};
+    int32_t *xmode[2] = {xpos, xi.data()};
+    int32_t **xind[1] = {xmode};
+    taco_tensor_t tx;
+    tx.indices = xind;
+    tx.vals = (float *)xv.data();
+    taco_tensor_t ty = dense_view(M, 1, y.data());
+    spmspv_csr_cpu_taco_ref(&ty, &tA, &tx);
+    wr(fo, y.data(), M);
   } else {
     fprintf(stderr, "unknown mode\n");
     return 2;

@@ -205,6 +205,7 @@ int run_spmm_planned(const SpmmPlan &plan, int M, int K, long long nnz, const in
   L.bulk_copies = plan.bulk_copies;
   L.deep = plan.deep;
   L.walk = plan.walk;
+  L.no_fork = plan.no_fork;
   const bool bf16 = b_dtype == SEGTACO_BF16;
   switch (plan.schedule) {
     case SEGTACO_RB_SR:

@@ -77,6 +77,8 @@ struct SpmmLaunch {
   int walk;                    // kWalkRows / kWalkRowsDeep / kWalkFlat (spmm_kernels.cuh)
   int long_row = 0;            // rb: rows of >= long_row nonzeros go to spmm_long.cu
   int carveout = -1;           // >= 0: preferred shared-memory carveout (%) of the launch
+  bool no_fork = false;        // rb long rows: both kernels on the call's stream (no side
+                               // stream or events are created)
 };
 // One launcher per (dense type, unit kind); each switches over (V, G).
 int launch_spmm_f32_rows(const SpmmLaunch &L, cudaStream_t s);
@@ -101,6 +103,7 @@ struct SpmmPlan {
   bool deep;
   int walk;                  // kWalkRows / kWalkRowsDeep / kWalkFlat
   int long_row;              // rb: long-row threshold (0: every row in the row-block kernel)
+  bool no_fork = false;      // rb long rows: no side stream (segtaco_spmm_noalloc)
   long long px_entries;      // int32 entries of the first workspace array (eb: chunk-edge
                              // rows; rb long rows: the list of long rows)
   long long py_entries;      // ... of the second (eb: chunk-edge nonzeros; long rows: counters)

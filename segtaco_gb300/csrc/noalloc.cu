@@ -14,6 +14,12 @@
 // call on each device this file looks up the array's device address with
 // cudaGetSymbolAddress, with that device current, and caches it per device.
 // That first call on a device should therefore come before any stream capture.
+// The cached address belongs to the device's primary context: after
+// cudaDeviceReset the module may load elsewhere, so resetting a device that
+// has served this entry point is not supported.  Besides the look-up, the
+// first call of a kernel variant may set its shared-memory attribute
+// (cudaFuncSetAttribute, the rb long-row CTAs); nothing else is created: the
+// long-row CTAs and the row-block kernel both run on the caller's stream.
 //
 // All calls share the one array: calls whose work overlaps on the GPU (on
 // different streams, or from different host threads without ordering) race on
@@ -75,6 +81,7 @@ extern "C" int segtaco_spmm_noalloc(int32_t M, int32_t K, int64_t nnz, const int
                      "segtaco_spmm_noalloc: PARTITION_READY is not supported (shared scratch)");
   SpmmPlan plan;
   SEGTACO_TRY(plan_spmm(M, K, nnz, N, b_dtype, ldb, ldc, B, C, cfg, &plan));
+  plan.no_fork = true;  // rb long rows: no side stream or events, both kernels on `stream`
   if (plan.long_row > 0 && plan.px_entries > kNoallocEntries) {
     // the long-row list would not fit: every row in the row-block kernel
     plan.long_row = 0;

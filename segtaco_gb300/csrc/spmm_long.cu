@@ -316,13 +316,26 @@ int launch_long_typed(const SpmmLaunch &L, const int *list, int *counters, int s
 }
 
 // Side stream and events of one host thread on one device, kept for the
-// thread's lifetime.
+// thread's lifetime and destroyed when the thread exits (a thread pool that
+// retires threads does not pile them up).  At process exit the CUDA runtime
+// may already be unloaded; the destroy calls then fail and are ignored.
 struct LongFork {
   cudaStream_t side = nullptr;
   cudaEvent_t start = nullptr, done = nullptr;
 };
 constexpr int kForkDevices = 64;
-thread_local LongFork t_forks[kForkDevices];
+struct LongForks {
+  LongFork dev[kForkDevices];
+  ~LongForks() {
+    for (LongFork &f : dev) {
+      if (f.side) cudaStreamDestroy(f.side);
+      if (f.start) cudaEventDestroy(f.start);
+      if (f.done) cudaEventDestroy(f.done);
+    }
+    cudaGetLastError();
+  }
+};
+thread_local LongForks t_forks;
 
 // The fork of this thread on the current device, created on first use (not
 // while `s` is being captured: then the caller runs both kernels on `s`).
@@ -333,7 +346,7 @@ LongFork *long_fork(cudaStream_t s) {
     return nullptr;
   }
   if (dev < 0 || dev >= kForkDevices) return nullptr;
-  LongFork &t_fork = t_forks[dev];
+  LongFork &t_fork = t_forks.dev[dev];
   if (t_fork.side) return &t_fork;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
@@ -393,7 +406,8 @@ int launch_spmm_long_rows(const SpmmLaunch &L, const int *list, int *counters, c
   // row-block kernel.
   SEGTACO_TRY(check_cuda(cudaMemsetAsync(counters + 2, 0, sizeof(unsigned long long), s),
                          "cudaMemsetAsync"));
-  LongFork *f = long_fork(s);
+  // segtaco_spmm_noalloc creates no side stream: both kernels go to `s`.
+  LongFork *f = L.no_fork ? nullptr : long_fork(s);
   cudaStream_t ls = f ? f->side : s;
   if (f) {
     SEGTACO_TRY(check_cuda(cudaEventRecord(f->start, s), "cudaEventRecord"));

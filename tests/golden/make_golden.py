@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this folder from segTACO's own CPU code.
 
-Run in a container that has the segTACO source tree (default /root/reference,
-override with SEGTACO_REFERENCE_TREE):
+Run where the segTACO source tree is present (oracle/build.py resolves its
+location; SEGTACO_REFERENCE_TREE overrides it):
 
     python tests/golden/make_golden.py
 
@@ -11,6 +11,8 @@ It builds oracle/_ref (oracle/build.py), feeds the seeded inputs below to
   SparseDenseProduct.h:109-146) and ``spmm_cpu_naive`` (spmm_csr_gpu.h:110-127)
 * ``ref_golden spmv``  -> Eigen ``EigenCSR * EigenVector``
 * ``ref_golden sddmm`` -> ``sddmm_csr_cpu_taco_ref`` (sddmm_csr_gpu.h:9-50), in double
+* ``ref_golden spmspv``-> ``spmspv_csr_cpu_taco_ref`` (spmspv_csr_gpu.h:9-32), in double,
+                          over A stored by columns (spmspv_csr_gpu.h:37-43)
 * ``ref_golden csr``   -> ``to_eigen_csr`` (ds.h:380-397) on an unsorted COO
 * ``ref_golden mtx``   -> ``read_mtx_file`` (ds.h:183-268) on the MatrixMarket
                           texts of ``mtx_texts()``
@@ -19,6 +21,10 @@ It builds oracle/_ref (oracle/build.py), feeds the seeded inputs below to
 
 and stores inputs and outputs as compressed .npz files.  Nothing at test time
 reads the reference tree; the tests only read these files.
+
+    python tests/golden/make_golden.py spmspv
+
+writes only the SpMSpV fixtures (the others are left as they are).
 """
 from __future__ import annotations
 
@@ -101,6 +107,60 @@ def spmm_cases():
     return cases
 
 
+def spmspv_cases():
+    """(A as CSR, x indices, x values): y = A x with A stored by columns.  The
+    reference driver draws x as a shuffled index list cut at 10 % of K with
+    values in [0, 1) (spmspv_csr_gpu.h:53-72); the cases keep that shape and
+    add the edges: empty columns, one long column, an empty x, x over all of K."""
+    cases = {}
+    rng = np.random.default_rng(51)
+
+    def x_of(K, frac, seed):
+        r = np.random.default_rng(seed)
+        idx = r.permutation(K)[: int(K * frac)].astype(np.int32)  # unsorted, distinct
+        return idx, r.uniform(0.0, 1.0, idx.shape[0]).astype(np.float32)
+
+    A = synth.random_csr(400, 350, 0.04, seed=52, p_empty=0.1)
+    cases["rand_nx10"] = (A, *x_of(A.K, 0.1, 53))
+    # every second column empty, x over all columns (half of them empty)
+    A = synth.random_csr(300, 200, 0.05, seed=54)
+    keep = (A.col % 2) == 0
+    rows = np.repeat(np.arange(A.M), A.row_lengths())[keep]
+    rp = np.zeros(A.M + 1, np.int64)
+    np.cumsum(np.bincount(rows, minlength=A.M), out=rp[1:])
+    A = synth.CSR(rp.astype(np.int32), A.col[keep], A.val[keep], A.M, A.K)
+    cases["empty_cols"] = (A, *x_of(A.K, 1.0, 55))
+    # one column holding 3,000 of the 3,000 rows, plus scattered others
+    A = synth.random_csr(3000, 64, 0.01, seed=56)
+    dense = np.zeros((A.M, A.K), bool)
+    dense[np.repeat(np.arange(A.M), A.row_lengths()), A.col] = True
+    dense[:, 17] = True
+    vals = rng.uniform(-1, 1, dense.shape).astype(np.float32)
+    A = synth.csr_from_dense_pattern(dense, vals)
+    idx, xv = x_of(A.K, 0.25, 57)
+    if 17 not in idx:
+        idx[0] = 17
+    cases["long_col"] = (A, idx, xv)
+    A = synth.random_csr(100, 120, 0.05, seed=58)
+    cases["empty_x"] = (A, np.zeros(0, np.int32), np.zeros(0, np.float32))
+    # power-law column lengths (the transpose of a power-law row matrix)
+    A = synth.power_law(2500, 2000, 1.8, 1500, 0.02, seed=59).transpose()
+    cases["powerlaw_cols_nx10"] = (A, *x_of(A.K, 0.1, 60))
+    return cases
+
+
+def make_spmspv(g, fin, fout):
+    for name, (A, idx, xv) in spmspv_cases().items():
+        At = A.transpose()  # CSC of A: col_ptr over K columns, row indices
+        _write(fin, np.array([A.M, A.K, A.nnz, idx.shape[0]], np.int64), At.row_ptr, At.col,
+               At.val.astype(np.float64), idx, xv.astype(np.float64))
+        _run(g, "spmspv", fin, fout)
+        y = np.fromfile(fout, np.float64)
+        assert y.shape[0] == A.M
+        np.savez_compressed(os.path.join(HERE, "spmspv_%s.npz" % name), col_ptr=At.row_ptr,
+                            row_idx=At.col, val=At.val, M=A.M, K=A.K, x_idx=idx, x_val=xv, y=y)
+
+
 def main():
     refs = obuild.build_ref()
     if not refs:
@@ -108,6 +168,10 @@ def main():
     g, s = refs["ref_golden"], refs["ref_search"]
     tmp = tempfile.mkdtemp(prefix="segtaco_golden_")
     fin, fout = os.path.join(tmp, "in.bin"), os.path.join(tmp, "out.bin")
+    make_spmspv(g, fin, fout)
+    if sys.argv[1:] == ["spmspv"]:
+        print("SpMSpV fixtures written to", HERE)
+        return
 
     # ---- SpMM + SpMV + searches -------------------------------------------
     out = {}

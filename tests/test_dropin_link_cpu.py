@@ -6,7 +6,7 @@ import subprocess
 
 import pytest
 
-REF_TREE = os.environ.get("SEGTACO_REFERENCE_TREE", "/root/reference")
+from oracle.build import REFERENCE_TREE as REF_TREE  # the recipe resolves the tree
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIBDIR = os.path.join(ROOT, "segtaco_gb300")
 

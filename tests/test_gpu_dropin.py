@@ -54,6 +54,20 @@ def test_sddmm_names(cuda, name):
     assert O.max_bound_err(out, d["out"], bound) <= TOL
 
 
+@pytest.mark.parametrize("case", ["rand_nx10", "long_col", "empty_cols"])
+def test_spmspv_name_golden(cuda, case):
+    """spmspv_csr_gpu_taco against segTACO's spmspv_csr_cpu_taco_ref output."""
+    d = load_golden("spmspv_", case)
+    M, K = int(d["M"]), int(d["K"])
+    y = np.full((M, 1), np.nan, np.float32)
+    tA, h1 = taco.csr(d["col_ptr"], d["row_idx"], d["val"], K, M)
+    tx, h2 = taco.sparse_vector(d["x_idx"], d["x_val"], K)
+    ty, h3 = taco.dense(y)
+    taco.call("spmspv_csr_gpu_taco", ty, tA, tx)
+    _, bound = O.spmspv_f64(d["col_ptr"], d["row_idx"], d["val"], M, d["x_idx"], d["x_val"])
+    assert O.max_bound_err(y.reshape(-1), d["y"], bound) <= TOL
+
+
 def test_spmspv_name(cuda):
     A = synth.random_csr(400, 300, 0.03, seed=21, p_empty=0.1)
     At = A.transpose()

@@ -137,6 +137,18 @@ def test_sddmm_bf16(cuda, D):
     check_vec(out.cpu().numpy(), ref, bound)
 
 
+@pytest.mark.parametrize("name", golden_cases("spmspv_"))
+def test_spmspv_golden(cuda, name):
+    """Against segTACO's own spmspv_csr_cpu_taco_ref output (tests/golden)."""
+    d = load_golden("spmspv_", name)
+    M = int(d["M"])
+    At = synth.CSR(d["col_ptr"], d["row_idx"], d["val"], int(d["K"]), M)
+    y = ops.spmspv(dev(At), torch.from_numpy(d["x_idx"]).cuda(),
+                   torch.from_numpy(d["x_val"]).cuda(), M).cpu().numpy()
+    _, bound = O.spmspv_f64(d["col_ptr"], d["row_idx"], d["val"], M, d["x_idx"], d["x_val"])
+    check_vec(y, d["y"], bound)
+
+
 @pytest.mark.parametrize("name", list(CASES))
 def test_spmspv(cuda, name):
     A = CASES[name]

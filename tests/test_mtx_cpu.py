@@ -13,7 +13,7 @@ from segtaco_gb300.mtx import read_mtx
 
 GOLD = np.load(os.path.join(os.path.dirname(__file__), "golden", "mtx_read.npz"))
 NAMES = sorted(k[len("text_"):] for k in GOLD.files if k.startswith("text_"))
-REF_TREE = os.environ.get("SEGTACO_REFERENCE_TREE", "/root/reference")
+from oracle.build import REFERENCE_TREE as REF_TREE  # the recipe resolves the tree
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 

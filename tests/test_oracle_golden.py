@@ -1,7 +1,7 @@
 """The CPU oracle pinned against segTACO's own code (golden fixtures made by
 tests/golden/make_golden.py from the reference's Eigen product,
-spmm_cpu_naive, sddmm_csr_cpu_taco_ref, to_eigen_csr and
-taco_binarySearchBefore/After)."""
+spmm_cpu_naive, sddmm_csr_cpu_taco_ref, spmspv_csr_cpu_taco_ref,
+to_eigen_csr and taco_binarySearchBefore/After)."""
 import numpy as np
 import pytest
 
@@ -10,10 +10,11 @@ from oracle import oracle as O
 
 SPMM = golden_cases("spmm_")
 SDDMM = golden_cases("sddmm_")
+SPMSPV = golden_cases("spmspv_")
 
 
 def test_fixture_inventory():
-    assert len(SPMM) >= 10 and len(SDDMM) >= 2
+    assert len(SPMM) >= 10 and len(SDDMM) >= 2 and len(SPMSPV) >= 5
 
 
 @pytest.mark.parametrize("name", SPMM)
@@ -115,3 +116,15 @@ def test_spmspv_oracle_matches_dense():
     dense = np.zeros((A.M, A.K))
     dense[np.repeat(np.arange(A.M), A.row_lengths()), A.col] = A.val
     assert np.allclose(y, dense @ x, rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", SPMSPV)
+def test_spmspv_oracle_matches_segtaco_bitexact(name):
+    """The FP64 restatement equals segTACO's spmspv_csr_cpu_taco_ref
+    (spmspv_csr_gpu.h:9-32) bit for bit: same x order, same column order,
+    multiply then add in double."""
+    d = load_golden("spmspv_", name)
+    y, bound = O.spmspv_f64(d["col_ptr"], d["row_idx"], d["val"], int(d["M"]), d["x_idx"],
+                            d["x_val"])
+    assert np.array_equal(y, d["y"])
+    assert np.all(bound >= np.abs(y))

@@ -47,13 +47,16 @@ def test_noalloc_matches_spmm_twice(cuda, sched):
 
 
 def test_noalloc_rejects_problems_beyond_its_scratch(cuda):
-    A = synth.power_law(20000, 18000, 1.8, 5000, 0.02, seed=33)
-    Ad = dev(A)
-    Bd = torch.zeros((A.K, 8), device="cuda")
-    Cd = torch.zeros((A.M, 8), device="cuda")
+    # 300,000 rows of one nonzero at one item per chunk: 600,000 chunks, more
+    # than twice the 262,143 the fixed scratch holds.
+    M = 300_000
+    rng = np.random.default_rng(33)
+    row_ptr = np.arange(M + 1, dtype=np.int32)
+    col = rng.integers(0, 1000, M, dtype=np.int32)
+    Ad = dev(synth.CSR(row_ptr, col, np.ones(M, np.float32), M, 1000))
+    Bd = torch.zeros((1000, 8), device="cuda")
+    Cd = torch.zeros((M, 8), device="cuda")
     cfg = N.Config.make(schedule="eb_pr", items_per_unit=1)  # one chunk per item
-    if A.M + A.nnz + 1 <= 262143:
-        pytest.skip("matrix too small to overflow the fixed scratch")
     st = _noalloc(Ad, Bd, Cd, cfg)
     assert st == N.EINVAL and "fixed scratch" in N.last_error()
 
@@ -63,7 +66,11 @@ def test_noalloc_rb_sr_long_rows(cuda):
     result stays the sequential FMA order, call after call."""
     from oracle import oracle as O
     A = synth.power_law(60_000, 50_000, 1.8, 40_000, 0.02, seed=35)
-    assert A.nnz >= 1_000_000 and A.row_lengths().max() >= 512
+    assert A.nnz >= 1_000_000 and A.row_lengths().max() >= 2048
+    # The long-row list (rows of >= 2048 nonzeros, two parts) fits the fixed
+    # scratch, so the long-row CTAs run rather than the row-block fallback.
+    hi, lo = A.nnz // (8 * 2048) + 1, A.nnz // 2048 + 1
+    assert hi + lo <= 262144
     B = synth.dense(A.K, 128, seed=36)
     Ad, Bd = dev(A), torch.from_numpy(B).cuda()
     want = O.spmm_f32_rowseq(A.row_ptr, A.col, A.val, B, fma=True)
