@@ -216,6 +216,29 @@ class ClockSampler:
                 "reasons": sorted(set().union(*(r[2] for r in use)))}
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), read only."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
+def cpu_baseline_build():
+    from oracle import build as obuild
+    return " ".join(obuild.timed_flags())
+
+
 def cpu_spmm_timed(A, B, reps, threads=0, frac=1.0):
     """Time the oracle's FP32 row-parallel product (segTACO's Eigen order) on
     the first `frac` of the rows; returns (seconds per rep, rows, nnz, threads)."""
@@ -321,6 +344,140 @@ def time_spmm(ops, N_, Ad, Bd, Cd, cfg, ws, stream, steps, warmup):
     return step, kern
 
 
+def sampled_spmm_err(A, B, C, rows):
+    """Max over `rows` of |c - c64| / sum_p |a_ip b_pk| (the tests' bound-
+    normalised error) against an FP64 product of A and B (host; fp32 values,
+    or bf16 values already widened).  C[k] is the computed row rows[k]."""
+    import numpy as np
+    worst = 0.0
+    for k, r in enumerate(rows):
+        s0, s1 = int(A.row_ptr[r]), int(A.row_ptr[r + 1])
+        a = A.val[s0:s1].astype(np.float64)
+        rb = B[A.col[s0:s1]].astype(np.float64)
+        exact = a @ rb
+        bound = np.abs(a) @ np.abs(rb)
+        err = np.abs(C[k].astype(np.float64) - exact) / np.maximum(bound, 1e-30)
+        worst = max(worst, float(err.max()) if err.size else 0.0)
+    return worst
+
+
+def sddmm_err(A, X, Y, out, esz, n=200_000, seed=8):
+    """Bound-normalised error of SDDMM results at `n` sampled nonzeros:
+    |o - o64| / (|a| sum_k |x_ik y_jk|), with X, Y the device factors (bf16
+    factors widened exactly)."""
+    import numpy as np
+    import torch
+    from segtaco_gb300 import synth
+    torch.cuda.synchronize()
+
+    def host(t):
+        if esz == 2:
+            return synth.bf16_bits_to_f32(t.view(torch.int16).cpu().numpy().view(np.uint16))
+        return t.cpu().numpy()
+    Xh, Yh = host(X).astype(np.float64), host(Y).astype(np.float64)
+    rng = np.random.default_rng(seed)
+    p = np.sort(rng.choice(A.nnz, min(n, A.nnz), replace=False))
+    rows = np.searchsorted(A.row_ptr, p, side="right") - 1
+    a = A.val[p].astype(np.float64)
+    xi, yj = Xh[rows], Yh[A.col[p]]
+    exact = a * np.einsum("ij,ij->i", xi, yj)
+    bound = np.abs(a) * np.einsum("ij,ij->i", np.abs(xi), np.abs(yj))
+    got = out.cpu().numpy()[p].astype(np.float64)
+    return float((np.abs(got - exact) / np.maximum(bound, 1e-30)).max())
+
+
+def vec_err(A, x, yd):
+    """Bound-normalised error of y = A x (device yd) against FP64:
+    max_i |y_i - y64_i| / sum_p |a_ip x_p|."""
+    import numpy as np
+    import scipy.sparse as sp
+    import torch
+    torch.cuda.synchronize()
+    S = sp.csr_matrix((A.val.astype(np.float64), A.col, A.row_ptr), shape=(A.M, A.K))
+    x64 = x.astype(np.float64)
+    exact = S @ x64
+    abs_S = sp.csr_matrix((np.abs(A.val.astype(np.float64)), A.col, A.row_ptr), shape=(A.M, A.K))
+    bound = abs_S @ np.abs(x64)
+    got = yd.cpu().numpy().astype(np.float64)
+    return float((np.abs(got - exact) / np.maximum(bound, 1e-30)).max())
+
+
+def rows_err(A, B, Cd, rows):
+    """sampled_spmm_err for the rows `rows` of the device result Cd."""
+    import torch
+    got = Cd.index_select(0, torch.from_numpy(rows.astype("int64")).to(Cd.device)).cpu().numpy()
+    return sampled_spmm_err(A, B, got, rows)
+
+
+def sample_rows(A, n=4096, longest=16, seed=7):
+    """`n` random rows plus the `longest` longest rows of A (sorted, distinct)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    lens = A.row_lengths()
+    pick = rng.choice(A.M, min(n, A.M), replace=False)
+    top = np.argsort(lens)[-longest:]
+    return np.unique(np.concatenate([pick, top]))
+
+
+def run_reference_gpu(args, N_, ops, stream, peak, A, B, C_ours=None):
+    """segTACO's own generic SpMM kernels (K15 rb_sr, K20 rb_pr, K24 eb_sr,
+    K30 eb_pr: dgSPARSE-style, any N <= 256) built for sm_103a from its
+    headers (baseline/ref_gpu.py) and called through its host wrappers, which
+    time {zero C, kernel} with its GPUTimer (get_gpu_timer_result).  Beside
+    them, this library's four schedules on the same operands, timed over the
+    same region (partition + product).  Runs on the headline workload (passed
+    in) and on the uniform 16384^2 SpMM (N = 32)."""
+    import numpy as np
+    import torch
+    from baseline import ref_gpu
+    if not ref_gpu.available():
+        return {"unavailable": "segTACO's GPU headers were not staged or the harness did not "
+                               "build (baseline/ref_gpu.py)"}
+    out = {"timer": "segTACO get_gpu_timer_result (zero C + kernel), median of 7 calls after 2; "
+                    "ours: partition + product, events on one stream",
+           "kernels": "K15 spmm_rb_sr, K20 spmm_rb_pr, K24 spmm_eb_sr, K30 spmm_eb_pr"}
+    from segtaco_gb300 import synth
+    cases = [("power_law", A, B, C_ours), ("uniform16", synth.uniform_rows(seed=0), None, None)]
+    for name, Ah, Bh, Cref in cases:
+        if Bh is None:
+            Bh = synth.dense(Ah.K, 32, seed=1)
+        N = Bh.shape[1]
+        byts = algorithmic_bytes(Ah.M, Ah.K, Ah.nnz, N)
+        try:
+            ref = ref_gpu.run(Ah, Bh, warmup=2, reps=7)
+        except Exception as exc:
+            out[name] = {"error": str(exc)[:300]}
+            continue
+        Ad = ops.DeviceCSR.from_host(Ah, "cuda")
+        Bd = torch.from_numpy(Bh).cuda()
+        Cd = torch.empty((Ah.M, N), dtype=torch.float32, device="cuda")
+        mx = int(Ah.row_lengths().max())
+        ent = {"M": Ah.M, "nnz": Ah.nnz, "N": N, "segtaco": {}, "ours": {}}
+        for s in ("rb_sr", "rb_pr", "eb_sr", "eb_pr"):
+            r = ref.get("spmm_" + s)
+            ms = statistics.median(r["ms"])
+            c = N_.Config.make(schedule=N_.SCHEDULES[s])
+            N_.check(N_.lib().segtaco_autotune_heuristic(Ah.M, Ah.K, Ah.nnz, N, N_.F32, mx, c))
+            w = torch.empty(max(256, ops.spmm_workspace_size(Ad, N, N_.F32, c)),
+                            dtype=torch.uint8, device="cuda")
+            st, kt = time_spmm(ops, N_, Ad, Bd, Cd, c, w, stream, 10, 3)
+            torch.cuda.synchronize()
+            ours_sum = float(Cd.double().sum().item())
+            err = rows_err(Ah, Bh, Cd, sample_rows(Ah, 2048))
+            ent.setdefault("max_err_vs_fp64", 0.0)
+            ent["max_err_vs_fp64"] = max(ent["max_err_vs_fp64"], err)
+            ent["segtaco"][s] = {"ms": round(ms, 4), "GBps": round(byts / ms / 1e6, 1),
+                                 "roofline_frac": round(byts / ms / 1e6 / peak, 4),
+                                 # checksum of segTACO's C against ours (same A, B)
+                                 "checksum_rel_diff": float("%.3g" % (
+                                     abs(r["checksum"] - ours_sum) / max(abs(ours_sum), 1e-30)))}
+            ent["ours"][s] = {"ms": round(st, 4), "speedup": round(ms / st, 2)}
+            del w
+        out[name] = ent
+        del Ad, Bd, Cd
+    return out
+
+
 def run_power_law_variant(args, N_, ops, stream, Bd, Cd, peak):
     """The power-law configuration at Zipf exponent 1.922 (1M x 1M, cap 50,000,
     2 % empty rows: 10,083,633 nonzeros, the "~10M" of the configuration's text,
@@ -400,8 +557,28 @@ def run_batched(args, N_, ops, stream, count=256):
 
     reps = max(3, args.steps // 4)
     t_call = timed(per_call, reps)
+    # the same per-call launches (partition + product per matrix) captured
+    # once into a CUDA graph and replayed: no host issue cost in the loop
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        per_call()
+
+    def replay():
+        with torch.cuda.stream(stream):  # the graph runs on the timed stream
+            g.replay()
+    t_call_graph = timed(replay, reps)
+    del g
     t_batch = timed(lambda: batch.run(stream=stream), reps)
     t_graph = timed(lambda: batch.run(stream=stream, graph=True), reps)
+    # measured error of a sample of the batched products against FP64
+    torch.cuda.synchronize()
+    worst = 0.0
+    for m in range(0, count, max(1, count // 8)):
+        Ad, B, C = items[m]
+        A_h, _, _ = synth.pool_matrix(m)
+        Bh = B.cpu().numpy()
+        worst = max(worst, rows_err(A_h, Bh, C, sample_rows(A_h, 512)))
     launches_call = sum(2 if c.schedule in (N_.EB_SR, N_.EB_PR) else 1 for c in cfgs)
     batch.close()
     scheds = {}
@@ -411,11 +588,17 @@ def run_batched(args, N_, ops, stream, count=256):
     return {
         "workload": "%d uneven matrices, M=K log-uniform [1e3, 2e5], row lengths lognormal "
                     "mean 12, N in {16,32,64,128}, FP32; %d nnz in all" % (count, nnz),
-        "metric": "SpMMs/s", "per_call_ms": round(t_call, 3), "batched_ms": round(t_batch, 3),
+        "metric": "SpMMs/s", "per_call_ms": round(t_call, 3),
+        "per_call_graph_ms": round(t_call_graph, 3),
+        "batched_ms": round(t_batch, 3),
         "batched_graph_ms": round(t_graph, 3),
-        "per_call_spmms_per_s": round(count / t_call * 1e3, 1),
+        "per_call_spmms_per_s": round(count / t_call_graph * 1e3, 1),
         "batched_spmms_per_s": round(count / t_graph * 1e3, 1),
-        "speedup_vs_per_call": round(t_call / t_graph, 3),
+        # against the per-call launches replayed from a graph (no host in the loop)
+        "speedup_vs_per_call": round(t_call_graph / t_graph, 3),
+        "speedup_vs_per_call_python_loop": round(t_call / t_graph, 3),
+        "max_err_vs_fp64": worst, "err_sample": "512 rows (incl. the 16 longest) of every "
+                                                "%d-th product" % max(1, count // 8),
         "batched_GBps": round(byts / t_graph / 1e6, 1),
         "per_call_launches": launches_call, "batched_launches": groups + 1,
         "batch_groups": groups, "queue_items": nitems, "schedules": scheds,
@@ -461,6 +644,8 @@ def run_side_ops(args, N_, ops, stream, A_pl, peak, A_host=None):
     out["spmv_power_law"] = {"ms": round(ms, 4), "GBps": round(byts / ms / 1e6, 1),
                              "roofline_frac": round(byts / ms / 1e6 / peak, 4),
                              "bytes": byts}
+    if A_host is not None:
+        out["spmv_power_law"]["max_err_vs_fp64"] = vec_err(A_host, x.cpu().numpy(), y)
     # bf16-B SpMM on the power-law matrix (N = 128, B 256 MB: beyond L2)
     bits = synth.to_bf16_bits(synth.dense(Ad.K, 128, seed=12))
     Bb = torch.from_numpy(bits.view(np.int16)).cuda().view(torch.bfloat16)
@@ -490,11 +675,14 @@ def run_side_ops(args, N_, ops, stream, A_pl, peak, A_host=None):
         ys = torch.empty(A_host.M, dtype=torch.float32, device="cuda")
         ms = _time_events(lambda: ops.spmspv(Atd, xi, xv, A_host.M, ys, stream=stream), stream,
                           reps)
+        xd = np.zeros(A_host.K, np.float32)
+        xd[xi_h] = xv.cpu().numpy()
+        spmspv_err = vec_err(A_host, xd, ys)
         colnnz = np.diff(At.row_ptr)[xi_h].astype(np.int64)
         byts = int(nx * 8 + (8 * nx + 8 * colnnz.sum()) + A_host.M * 4)
         out["spmspv_power_law"] = {"ms": round(ms, 4), "GBps": round(byts / ms / 1e6, 1),
                                    "roofline_frac": round(byts / ms / 1e6 / peak, 4),
-                                   "bytes": byts, "nx": nx}
+                                   "bytes": byts, "nx": nx, "max_err_vs_fp64": spmspv_err}
         del Atd
     # banded-plus-random: SDDMM and SpMM, fp32 and bf16 dense operands
     A = synth.banded_plus_random(seed=0)
@@ -511,7 +699,8 @@ def run_side_ops(args, N_, ops, stream, A_pl, peak, A_host=None):
         byts = A.nnz * 12 + (A.M + 1) * 4 + (A.M + A.K) * D * esz
         out["sddmm_banded_" + name] = {"ms": round(ms, 4), "GBps": round(byts / ms / 1e6, 1),
                                        "roofline_frac": round(byts / ms / 1e6 / peak, 4),
-                                       "bytes": byts}
+                                       "bytes": byts,
+                                       "max_err_vs_fp64": sddmm_err(A, X, Y, o, esz)}
         Bm = conv(synth.dense(A.K, D, seed=6))
         Cm = torch.empty((A.M, D), dtype=torch.float32, device="cuda")
         cfg = N_.Config.make(schedule=N_.AUTO)
@@ -526,25 +715,16 @@ def run_side_ops(args, N_, ops, stream, A_pl, peak, A_host=None):
         ent = {"ms": round(ms, 4), "GBps": round(byts / ms / 1e6, 1),
                "roofline_frac": round(byts / ms / 1e6 / peak, 4), "bytes": byts,
                "schedule": {v: k for k, v in N_.SCHEDULES.items()}[cfg.schedule]}
+        # error against FP64 over sampled rows (bf16: of the same bf16 values)
+        torch.cuda.synchronize()
+        rows = sample_rows(A, 4096)
         if esz == 2:
-            # error of the bf16-B product against FP64 over sampled rows
-            torch.cuda.synchronize()
-            rng = np.random.default_rng(7)
-            rows = np.sort(rng.choice(A.M, 4096, replace=False))
             Bh = Bm.view(torch.int16).cpu().numpy().view(np.uint16)
             Bf = synth.bf16_bits_to_f32(Bh).astype(np.float64)
-            Ch = Cm.cpu().numpy()
-            worst = 0.0
-            for r in rows:
-                s0, s1 = A.row_ptr[r], A.row_ptr[r + 1]
-                a = A.val[s0:s1].astype(np.float64)
-                rowsB = Bf[A.col[s0:s1]]
-                exact = a @ rowsB
-                bound = np.abs(a) @ np.abs(rowsB)
-                err = np.abs(Ch[r] - exact) / np.maximum(bound, 1e-30)
-                worst = max(worst, float(err.max()))
-            ent["max_err_vs_fp64_bf16_values"] = worst
-            ent["tolerance"] = 1e-5
+            ent["max_err_vs_fp64_bf16_values"] = rows_err(A, Bf, Cm, rows)
+        else:
+            ent["max_err_vs_fp64"] = rows_err(A, Bm.cpu().numpy(), Cm, rows)
+        ent["tolerance"] = 1e-5
         out["spmm_banded_" + name] = ent
     out["config"] = ("SpMV and SpMSpV (x 10%% nonzero): power-law 1Mx1M (%d nnz); "
                      "banded-plus-random %dx%d, %d nnz, D=N=64" % (Ad.nnz, A.M, A.K, A.nnz))
@@ -647,6 +827,43 @@ def serving_stream(n_req, pool_size=1024, lam=20000.0, recent=8, p_repeat=0.8, s
 _POOL_CACHE = {}  # pool matrices of a request stream, shared by the fp32 and bf16 runs
 
 
+def served_err(args, N_, mats, ids, is_spmm, count=32):
+    """Bound-normalised error against FP64 of served results: the stream's
+    first `count` requests (SpMM and SDDMM, device-resident fp32 operands),
+    submitted at once to a fresh server so that they batch together."""
+    import numpy as np
+    import torch
+    from segtaco_gb300 import synth
+    from segtaco_gb300.serving import Server
+    worst, keep = 0.0, []
+    with Server(slots=args.serve_slots, max_batch=args.serve_max_batch) as srv:
+        for m in sorted(set(ids[:count])):
+            srv.add_matrix(m, mats[m][0], pin=True)
+        tickets = []
+        for k in range(count):
+            A, n, _ = mats[ids[k]]
+            X = torch.from_numpy(synth.dense(A.M if not is_spmm[k] else A.K, n, seed=90 + k)).cuda()
+            if is_spmm[k]:
+                out = torch.empty((A.M, n), dtype=torch.float32, device="cuda")
+                tickets.append(srv.spmm(ids[k], X, out, device=True))
+                keep.append((k, X, None, out))
+            else:
+                Y = torch.from_numpy(synth.dense(A.K, n, seed=190 + k)).cuda()
+                out = torch.empty(A.nnz, dtype=torch.float32, device="cuda")
+                tickets.append(srv.sddmm(ids[k], X, Y, out, device=True))
+                keep.append((k, X, Y, out))
+        bad = sum(1 for t in tickets if srv.wait(t, -1) != N_.OK)
+        if bad:
+            return float("inf")
+    for k, X, Y, out in keep:
+        A = mats[ids[k]][0]
+        if Y is None:
+            worst = max(worst, rows_err(A, X.cpu().numpy(), out, sample_rows(A, 1024)))
+        else:
+            worst = max(worst, sddmm_err(A, X, Y, out, 4, n=50_000))
+    return worst
+
+
 def run_serving(args, N_, n_req=2000, bf16=False, device=False):
     """Served SpMM/SDDMM stream through segtaco_server (continuous batching over
     a device CSR cache), against the same stream in per-call mode (one request
@@ -726,6 +943,10 @@ def run_serving(args, N_, n_req=2000, bf16=False, device=False):
                         "batches": st["batches"], "span_ms": round(st["span_s"] * 1e3, 2),
                         "burst_requests_per_s": round(sb["completed"] / sb["span_s"], 1),
                         "failed": bad}
+    if device and not bf16:
+        result["max_err_vs_fp64"] = served_err(args, N_, mats, ids, is_spmm)
+        result["err_sample"] = ("the first 32 requests of the stream, submitted together to a "
+                                "fresh server (batched in the mix), each to its own output")
     result["throughput_vs_per_call"] = round(result["batched"]["requests_per_s"] /
                                              result["per_call"]["requests_per_s"], 3)
     result["p99_vs_per_call"] = round(result["per_call"]["p99_us"] /
@@ -733,6 +954,69 @@ def run_serving(args, N_, n_req=2000, bf16=False, device=False):
     result["capacity_vs_per_call"] = round(result["batched"]["burst_requests_per_s"] /
                                            result["per_call"]["burst_requests_per_s"], 3)
     return result
+
+
+def compact_summary(d):
+    """The headline's context in a few hundred bytes: per-schedule kernel ms,
+    roofline fraction and error vs FP64; segTACO's own GPU kernels and
+    cuSPARSE on the same operands; batched and served ratios; side ops."""
+    def r(x, n=4):
+        return None if x is None else round(x, n)
+    out = {}
+    if d.get("schedules"):
+        out["schedules"] = {k: [v["kernel_ms"], v["roofline_frac"], float("%.2g" % v["max_err_vs_fp64"])]
+                            for k, v in d["schedules"].items()}
+        out["schedules_fields"] = ["kernel_ms", "roofline_frac", "max_err_vs_fp64"]
+    v = d.get("power_law_10m")
+    if v:
+        out["power_law_10m_ms"] = {k: x["kernel_ms"] for k, x in v["schedules"].items()}
+        out["power_law_10m_ms"]["spmv"] = v["spmv"]["ms"]
+    rg = d.get("reference_gpu")
+    if rg:
+        if "unavailable" in rg:
+            out["segtaco_gpu"] = rg["unavailable"]
+        for w in ("power_law", "uniform16"):
+            e = rg.get(w)
+            if e and "segtaco" in e:
+                out["segtaco_gpu_ms_vs_ours_" + w] = {
+                    k: [e["segtaco"][k]["ms"], e["ours"][k]["ms"]] for k in e["segtaco"]}
+                if w == "uniform16":
+                    out["uniform16_max_err_vs_fp64"] = float("%.2g" % e.get("max_err_vs_fp64", 0))
+            elif e:
+                out["segtaco_gpu_" + w] = e
+    if d.get("vendor") and "ms_per_step" in d["vendor"]:
+        out["cusparse_ms"] = d["vendor"]["ms_per_step"]
+    b = d.get("batched")
+    if b:
+        out["batched"] = {"speedup_vs_per_call_graph": b["speedup_vs_per_call"],
+                          "per_call_graph_ms": b["per_call_graph_ms"],
+                          "per_call_python_ms": b["per_call_ms"],
+                          "batched_graph_ms": b["batched_graph_ms"],
+                          "max_err_vs_fp64": float("%.2g" % b["max_err_vs_fp64"])}
+    sv = d.get("served")
+    if sv:
+        def one(x):
+            return [x["batched"]["requests_per_s"], x["per_call"]["requests_per_s"],
+                    x["batched"]["p50_us"], x["batched"]["p99_us"], x["per_call"]["p99_us"],
+                    x["capacity_vs_per_call"]]
+        out["served_fields"] = ["req_per_s", "per_call_req_per_s", "p50_us", "p99_us",
+                                "per_call_p99_us", "capacity_vs_per_call"]
+        out["served"] = {"fp32_host": one(sv)}
+        for k, n in (("bf16_operands", "bf16_host"), ("device_operands", "fp32_device")):
+            if sv.get(k):
+                out["served"][n] = one(sv[k])
+                if "max_err_vs_fp64" in sv[k]:
+                    out["served_max_err_vs_fp64"] = float("%.2g" % sv[k]["max_err_vs_fp64"])
+    so = d.get("side_ops")
+    if so:
+        out["side_ops"] = {}
+        for k, x in so.items():
+            if isinstance(x, dict) and "ms" in x:
+                err = x.get("max_err_vs_fp64", x.get("max_err_vs_fp64_bf16_values"))
+                out["side_ops"][k] = [x["ms"], x["roofline_frac"]] + (
+                    [float("%.2g" % err)] if err is not None else [])
+        out["side_ops_fields"] = ["ms", "roofline_frac", "max_err_vs_fp64"]
+    return out
 
 
 def run_ours(args, world, rank, local):
@@ -779,6 +1063,7 @@ def run_ours(args, world, rank, local):
 
     # per-schedule sweep (context for the headline; same workload)
     schedules = {}
+    err_rows = sample_rows(A, 4096)  # 4,096 random rows and the 16 longest
     if args.all_schedules:
         for s in ("rb_sr", "rb_pr", "eb_sr", "eb_pr"):
             c = tuned(N_.SCHEDULES[s])
@@ -786,10 +1071,12 @@ def run_ours(args, world, rank, local):
             wsz = max(256, ops.spmm_workspace_size(Ad, N, N_.F32, c))
             w = torch.empty(wsz, dtype=torch.uint8, device="cuda")
             st, kt = time_spmm(ops, N_, Ad, Bd, Cd, c, w, stream, max(3, args.steps // 2), 2)
+            torch.cuda.synchronize()
             schedules[s] = {"config": {k: v for k, v in c.as_dict().items() if v},
                             "ms_per_step": round(st, 4), "kernel_ms": round(kt, 4),
                             "GBps": round(byts / st / 1e6, 1),
-                            "roofline_frac": round(byts / kt / 1e6 / peak, 4)}
+                            "roofline_frac": round(byts / kt / 1e6 / peak, 4),
+                            "max_err_vs_fp64": rows_err(A, B, Cd, err_rows)}
             del w
 
     # the same configuration at the exponent that gives ~10M nonzeros
@@ -881,6 +1168,9 @@ def run_ours(args, world, rank, local):
     if not args.no_probe:
         ceiling = run_gather_ceiling(ops, stream)
         link = run_link_probe(stream)
+    ref_gpu = None
+    if not args.no_ref_gpu and args.workload == "power_law":
+        ref_gpu = run_reference_gpu(args, N_, ops, stream, peak, A, B)
 
     cpu = None  # the CPU baseline runs at N = 1 only (rank 0 of a single rank)
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -888,13 +1178,20 @@ def run_ours(args, world, rank, local):
         t1, _, _, _ = cpu_spmm_timed(A, B, 1)
         reps = int(min(60, max(2, round(10.0 / max(t1, 1e-3)))))
         sec, Ms, nnzs, threads = cpu_spmm_timed(A, B, reps)
+        # one thread on the first rows (about 3 s), scaled by the nonzeros it covers
+        frac1 = min(1.0, max(0.01, 3.0 / max(t1 * threads, 1e-3)))
+        sec1, M1, nnz1, _ = cpu_spmm_timed(A, B, 1, threads=1, frac=frac1)
         cpu = {"value": round(byts * (nnzs / A.nnz) / sec / 1e9, 3), "unit": UNIT,
-               "cores": threads, "kind": "port",
+               "cores": threads, "kind": "port", "cpu_model": cpu_model(),
                "sample": "full workload, median of %d runs after warm-up (%.3f s each, %.1f s "
-                         "in all)" % (reps, sec, reps * sec)}
+                         "in all)" % (reps, sec, reps * sec),
+               "one_thread": {"value": round(byts * (nnz1 / A.nnz) / sec1 / 1e9, 3),
+                              "sample": "rows [0, %d) (%.1f%% of nonzeros), one run after "
+                                        "warm-up" % (M1, 100.0 * nnz1 / A.nnz)},
+               "build": cpu_baseline_build()}
 
     if rank == 0:
-        line = {
+        detail = {
             "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -926,8 +1223,18 @@ def run_ours(args, world, rank, local):
             "power_law_10m": variant,
             "vendor": vendor, "batched": batched, "served": served,
             "gather_ceiling": ceiling, "link": link, "side_ops": side,
+            "reference_gpu": ref_gpu,
         }
-        print(json.dumps(line), flush=True)
+        # Everything measured, on one line that is not the result line ...
+        print("# detail " + json.dumps(detail), flush=True)
+        # ... then the result line last and compact, so that a reader of the
+        # last few KB of output sees it whole.
+        line = {k: detail[k] for k in (
+            "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+            "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config", "roofline",
+            "gpu_launches", "e2e", "cpu_baseline", "clocks")}
+        line["summary"] = compact_summary(detail)
+        print(json.dumps(line, separators=(",", ":")), flush=True)
 
 
 def main():
@@ -961,6 +1268,8 @@ def main():
     ap.add_argument("--serve-max-batch", type=int, default=64, help="serving: requests per batch")
     ap.add_argument("--no-probe", action="store_true")
     ap.add_argument("--no-side-ops", action="store_true")
+    ap.add_argument("--no-ref-gpu", action="store_true",
+                    help="skip timing segTACO's own GPU kernels (baseline/ref_gpu.py)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup(args)

@@ -1,9 +1,10 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
 * ``build_oracle()`` compiles ``segtaco_oracle.c`` (exact restatement, built with
-  ``-ffp-contract=off``) and ``segtaco_cpu_baseline.c`` (the timed CPU baseline)
-  into ``oracle/_build/liboracle.so`` with gcc + OpenMP.  Portable flags only, so
-  the same recipe works on x86-64 and aarch64 hosts.
+  ``-ffp-contract=off``, portable flags) and ``segtaco_cpu_baseline.c`` (the
+  timed CPU baseline, ``timed_flags()``: -O3, OpenMP, Grace-tuned on Grace)
+  into ``oracle/_build/liboracle.so`` with gcc.  The same recipe works on
+  x86-64 and aarch64 hosts.
 * ``build_ref()`` compiles segTACO's own CPU code from the reference source tree
   (when that tree is present) into ``oracle/_ref/``: ``ref_golden`` (Eigen
   product, spmm_cpu_naive, the SDDMM and SpMSpV CPU references, the .mtx reader)
@@ -38,6 +39,24 @@ def _stale(target, sources):
     return any(os.path.getmtime(s) > t for s in sources)
 
 
+def timed_flags() -> list:
+    """Flags of the timed CPU baseline: -O3 with OpenMP, tuned for the host's
+    cores where they are Grace's (Neoverse V2: -mcpu=neoverse-v2 names that
+    core explicitly); elsewhere portable.  The exact restatement keeps
+    portable flags and -ffp-contract=off (its results are compared bit for
+    bit; the timed product's are not)."""
+    import platform
+    flags = ["-O3", "-fopenmp"]
+    if platform.machine() in ("aarch64", "arm64"):
+        try:
+            part = [l for l in open("/proc/cpuinfo") if l.lower().startswith("cpu part")]
+        except OSError:
+            part = []
+        if part and part[0].split(":")[1].strip().lower() == "0xd4f":  # Neoverse V2
+            flags.append("-mcpu=neoverse-v2")
+    return flags
+
+
 def build_oracle(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     exact = os.path.join(HERE, "segtaco_oracle.c")
@@ -47,7 +66,7 @@ def build_oracle(force: bool = False) -> str:
     o1 = os.path.join(BUILD, "segtaco_oracle.o")
     o2 = os.path.join(BUILD, "segtaco_cpu_baseline.o")
     _run(["gcc", "-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-std=gnu11", "-c", exact, "-o", o1])
-    _run(["gcc", "-O3", "-fPIC", "-fopenmp", "-std=gnu11", "-c", timed, "-o", o2])
+    _run(["gcc", *timed_flags(), "-fPIC", "-std=gnu11", "-c", timed, "-o", o2])
     tmp = LIB + ".tmp"
     _run(["gcc", "-shared", "-fopenmp", o1, o2, "-o", tmp, "-lm"])
     os.replace(tmp, LIB)
@@ -112,6 +131,14 @@ def build_ref(force: bool = False) -> dict:
               golden_src, "-o", golden_bin,
               "-Wl,--unresolved-symbols=ignore-all"])
     out["ref_golden"] = golden_bin
+    # Eigen's product timed with the timed port's flags (-O3, OpenMP, portable)
+    time_src = os.path.join(HERE, "ref", "ref_eigen_time.cpp")
+    time_bin = os.path.join(REF_OUT, "ref_eigen_time")
+    if force or _stale(time_bin, [time_src, __file__]):
+        _run(["g++", "-O3", "-std=c++14", "-fopenmp", "-w", "-DNDEBUG",
+              "-I", REFERENCE_TREE, "-I", os.path.join(REFERENCE_TREE, "eigen-3.4.0"),
+              "-I", "/usr/local/cuda/include", time_src, "-o", time_bin])
+    out["ref_eigen_time"] = time_bin
     search_src = os.path.join(HERE, "ref", "ref_search.cu")
     search_bin = os.path.join(REF_OUT, "ref_search")
     if force or _stale(search_bin, [search_src, __file__]):

@@ -102,6 +102,9 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
       // A requested slab width picks the vector width (W = 32*V).
       while (V > 1 && 32 * V > c.col_tile) V >>= 1;
     }
+    // No idle half-slab: N = 32 takes one column per lane, not 8 lanes of 4.
+    if (c.vec <= 0)
+      while (V > 1 && 32 * (V / 2) >= N) V >>= 1;
   } else {
     int W = c.col_tile > 0 ? c.col_tile : 128 / esz;
     if (V > 8 && W / V > 4) V = 8;  // 16-element lanes: G <= 4
@@ -281,9 +284,14 @@ int segtaco_autotune_heuristic(int32_t M, int32_t K, int64_t nnz, int32_t N, int
   // vectors on all 32 lanes).  A B that fits L2 whole is one slab.
   const double bbytes = (double)K * N * esz;
   const bool skewed = mean > 0.0 && (double)max_row_len > 8.0 * mean;
-  if (sequential)
-    cfg->col_tile = 32 * (16 / esz);
-  else
+  if (sequential) {
+    // The narrowest lanes that still cover N in one slab (N = 32: one column
+    // per lane, all 32 lanes busy; measured on GB300, 16,384^2 with 16
+    // nonzeros per row, N = 32: 16-byte lanes left 24 of 32 lanes idle).
+    int v = 16 / esz;
+    while (v > 1 && 32 * (v / 2) >= N) v >>= 1;
+    cfg->col_tile = 32 * v;
+  } else
     cfg->col_tile = bbytes <= 48e6 ? (N <= 64 * 4 / esz ? N : 64 * 4 / esz) : 128 / esz;
   // Row-block schedules from 1M nonzeros whose longest row reaches the
   // long-row threshold hand those rows to CTAs of their own (spmm_long.cu;

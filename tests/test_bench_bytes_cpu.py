@@ -30,3 +30,32 @@ def test_workloads():
     assert (A.M, A.K, A.nnz, N, B.shape) == (16384, 16384, 262_144, 32, (16384, 32))
     A, B, N, desc = bench.make_workload("power_law_10m")
     assert (A.M, A.nnz, N) == (1_000_000, 10_083_633, 128) and "1.922" in desc
+
+
+def test_result_line_is_compact():
+    """The result line (printed last) carries the contract keys and a summary
+    that stays under 3 KB for a fully populated measurement."""
+    import json
+    sched = {k: {"kernel_ms": 1.1234, "roofline_frac": 0.1591, "max_err_vs_fp64": 3.1e-7,
+                 "config": {"schedule": 3}} for k in ("rb_sr", "rb_pr", "eb_sr", "eb_pr")}
+    served = {"batched": {"requests_per_s": 19999.9, "p50_us": 75.1, "p99_us": 510.2},
+              "per_call": {"requests_per_s": 5000.1, "p99_us": 15000.2},
+              "capacity_vs_per_call": 4.12}
+    ref = {"segtaco": {k: {"ms": 3.2} for k in sched}, "ours": {k: {"ms": 1.1} for k in sched},
+           "max_err_vs_fp64": 1e-7}
+    d = {"schedules": sched,
+         "power_law_10m": {"schedules": sched, "spmv": {"ms": 0.088}},
+         "reference_gpu": {"power_law": ref, "uniform16": ref},
+         "vendor": {"ms_per_step": 2.2},
+         "batched": {"speedup_vs_per_call": 3.2, "per_call_graph_ms": 11.9, "per_call_ms": 12.0,
+                     "batched_graph_ms": 3.7, "max_err_vs_fp64": 2e-7},
+         "served": dict(served, bf16_operands=served,
+                        device_operands=dict(served, max_err_vs_fp64=1e-7)),
+         "side_ops": {k: {"ms": 0.1234, "roofline_frac": 0.2034, "max_err_vs_fp64": 1e-7}
+                      for k in ("spmv_power_law", "spmm_power_law_bf16", "spmspv_power_law",
+                                "sddmm_banded_f32", "sddmm_banded_bf16", "spmm_banded_f32",
+                                "spmm_banded_bf16")}}
+    s = bench.compact_summary(d)
+    assert len(json.dumps(s, separators=(",", ":"))) < 2200
+    assert s["batched"]["speedup_vs_per_call_graph"] == 3.2
+    assert set(s["schedules"]) == {"rb_sr", "rb_pr", "eb_sr", "eb_pr"}

@@ -212,6 +212,12 @@ def test_workspace_and_heuristic(native_lib):
     assert L.segtaco_autotune_heuristic(10**6, 10**6, 2 * 10**7, 128, N.BF16, 48679,
                                         C.byref(h)) == N.OK
     assert h.col_tile == 128
+    for n, tile in ((32, 32), (16, 32), (64, 64), (33, 64), (100, 128)):
+        for sched in (N.RB_SR, N.EB_SR):  # sequential: the narrowest lanes covering N
+            h.schedule = sched
+            assert L.segtaco_autotune_heuristic(16384, 16384, 262144, n, N.F32, 16,
+                                                C.byref(h)) == N.OK
+            assert h.col_tile == tile, (sched, n, h.col_tile)
 
 
 def test_autotune_from_a_host_csr(native_lib):
