@@ -703,10 +703,9 @@ def run_side_ops(args, N_, ops, stream, A_pl, peak, A_host=None):
                                        "max_err_vs_fp64": sddmm_err(A, X, Y, o, esz)}
         Bm = conv(synth.dense(A.K, D, seed=6))
         Cm = torch.empty((A.M, D), dtype=torch.float32, device="cuda")
-        cfg = N_.Config.make(schedule=N_.AUTO)
-        N_.check(N_.lib().segtaco_autotune_heuristic(A.M, A.K, A.nnz, D,
-                                                    N_.F32 if esz == 4 else N_.BF16,
-                                                    int(A.row_lengths().max()), cfg))
+        # the library's choice from device statistics (row lengths, nonzeros
+        # near the diagonal: the staged B window for this banded matrix)
+        cfg = ops.autotune(Bd, D, N_.F32 if esz == 4 else N_.BF16)
         wsz = max(256, ops.spmm_workspace_size(Bd, D, N_.F32 if esz == 4 else N_.BF16, cfg))
         w = torch.empty(wsz, dtype=torch.uint8, device="cuda")
         ms = _time_events(lambda: ops.spmm(Bd, Bm, C_out=Cm, config=cfg, workspace=w,
@@ -714,7 +713,8 @@ def run_side_ops(args, N_, ops, stream, A_pl, peak, A_host=None):
         byts = algorithmic_bytes(A.M, A.K, A.nnz, D, esz)
         ent = {"ms": round(ms, 4), "GBps": round(byts / ms / 1e6, 1),
                "roofline_frac": round(byts / ms / 1e6 / peak, 4), "bytes": byts,
-               "schedule": {v: k for k, v in N_.SCHEDULES.items()}[cfg.schedule]}
+               "schedule": {v: k for k, v in N_.SCHEDULES.items()}[cfg.schedule],
+               "plan": ops.plan_name(Bd, Bm, cfg)}
         # error against FP64 over sampled rows (bf16: of the same bf16 values)
         torch.cuda.synchronize()
         rows = sample_rows(A, 4096)

@@ -80,6 +80,16 @@ extern "C" {
                                       segtaco_autotune_heuristic sets it when
                                       the longest row reaches that length      */
 
+#define SEGTACO_FLAG_WINDOW 128u /* rb schedules: each CTA of 4 * rows_per_unit rows
+                                     stages the B rows [i0 - H, i1 + H) of its column
+                                     slab in shared memory with one TMA tensor copy
+                                     and gathers rows inside that window from it
+                                     (H = items_per_unit; 0 = 32); for matrices
+                                     whose nonzeros lie near the diagonal.  Needs B
+                                     16-byte aligned, ldb * element size a multiple
+                                     of 16 and 4 * rows_per_unit + 2H <= 256;
+                                     otherwise ignored.  Not with LONG_ROWS     */
+
 /* Tuning knobs.  Zero in a field means "choose automatically". */
 typedef struct segtaco_config {
   int32_t schedule;       /* SEGTACO_RB_SR .. SEGTACO_EB_PR, or SEGTACO_AUTO    */
@@ -113,11 +123,22 @@ const char *segtaco_last_error(void);
 int segtaco_device_available(void);
 
 /* Fill *cfg with the automatic choice for this shape (host-side statistics
- * only: M, K, nnz, N, and optionally max/mean row length if known >= 0). */
+ * only: M, K, nnz, N, and optionally max/mean row length if known >= 0).
+ * On input, cfg->schedule may request a schedule (else SEGTACO_AUTO) and
+ * cfg->flags & SEGTACO_FLAG_WINDOW says that most nonzeros lie within 32 of
+ * the diagonal (segtaco_band_stats): row-block schedules then get the staged
+ * B window.  Every other input field is ignored and overwritten. */
 int segtaco_autotune_heuristic(int32_t M, int32_t K, int64_t nnz, int32_t N, int32_t b_dtype,
                                int64_t max_row_len, segtaco_config *cfg);
 
 /* ---- SpMM: C = A * B  (the segTACO hot path) --------------------------- */
+/* The plan segtaco_spmm would run for these arguments, as text: schedule,
+ * kernel (rows, chunks, long_rows, window, tma_ring), lanes V x G, slab width
+ * W, slabs, walk, window halo, rows per unit.  C is taken as dense (ldc = N,
+ * aligned); B's alignment and ldb matter. */
+int segtaco_spmm_plan_name(int32_t M, int32_t K, int64_t nnz, int32_t N, int32_t b_dtype,
+                           const void *B, int64_t ldb, const segtaco_config *cfg, char *out,
+                           size_t len);
 int segtaco_spmm_workspace_size(int32_t M, int32_t K, int64_t nnz, int32_t N, int32_t b_dtype,
                                 const segtaco_config *cfg, size_t *bytes);
 int segtaco_spmm(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr, const int32_t *col,
@@ -335,6 +356,11 @@ void segtaco_host_csr_free(segtaco_host_csr *csr);
  * stats[0] max row length, [1] empty rows, [2] rows >= 32, [3] nonzeros in
  * rows >= 32.  Synchronises `stream`. */
 int segtaco_row_stats(int32_t M, const int32_t *row_ptr, int64_t *stats, void *stream);
+/* Number of nonzeros of A (device CSR) within `halo` columns of the diagonal
+ * (row i against column i*K/M), into *in_band (host).  Synchronises `stream`.
+ * The autotuner's locality test for SEGTACO_FLAG_WINDOW. */
+int segtaco_band_stats(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr,
+                       const int32_t *col, int32_t halo, int64_t *in_band, void *stream);
 
 /* ---- partition arrays (exported so they can be checked bit-exactly) ---- */
 /* segTACO's block starts: out[b] = taco_binarySearchBefore(row_ptr, 0, M, b*P)
@@ -368,6 +394,39 @@ int segtaco_spmv(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr, cons
 int segtaco_sddmm(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr, const int32_t *col,
                   const float *vals, const void *X, const void *Y, int32_t x_dtype, int64_t ldx,
                   int64_t ldy, int32_t D, float *out, void *stream);
+
+/* SDDMM kernels: element-balanced blocks of nonzeros, one per warp; the
+ * fixed-shape kernel (each dot product split over `lanes` lanes with one or
+ * two 32-byte, or up to four 16-byte, loads of X[i] and Y[j] per lane) where
+ * D and the operands' alignment allow it, else the general kernel (V-wide
+ * vectors, lanes covering D) -- segTACO's two schedules are the row-warp
+ * sddmm_csr_gpu_warp and the element-balanced sddmm_csr_gpu_taco
+ * (sddmm_csr_gpu_taco.h:46-68, 120-148). */
+#define SEGTACO_SDDMM_AUTO 0
+#define SEGTACO_SDDMM_FIXED 1
+#define SEGTACO_SDDMM_GENERAL 2
+typedef struct segtaco_sddmm_config {
+  int32_t kernel;     /* SEGTACO_SDDMM_AUTO / _FIXED / _GENERAL                     */
+  int32_t block_nnz;  /* nonzeros per warp block, a power of two 32 .. 4096 (0: 256) */
+  int32_t lanes;      /* lanes per dot product (0: from D; power of two); a count
+                         the fixed kernel has no shape for (one 32-byte load per
+                         lane, two from 4 lanes, or four 16-byte loads) is
+                         ignored                                               */
+  int32_t reserved;
+} segtaco_sddmm_config;
+/* The library's SDDMM configuration for this shape: the block size so that a
+ * small problem still fills the GPU (at least two waves of warps), the lanes
+ * per dot product from D, the element type and the row lengths (rows of a
+ * few nonzeros reuse X[i] little, so fewer lanes with more loads each).
+ * max_row_len < 0 if unknown. */
+int segtaco_sddmm_autotune(int32_t M, int32_t K, int64_t nnz, int32_t D, int32_t x_dtype,
+                           int64_t max_row_len, segtaco_sddmm_config *cfg);
+/* segtaco_sddmm with an explicit configuration (NULL: segtaco_sddmm_autotune
+ * on the shape alone). */
+int segtaco_sddmm_ex(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr,
+                     const int32_t *col, const float *vals, const void *X, const void *Y,
+                     int32_t x_dtype, int64_t ldx, int64_t ldy, int32_t D, float *out,
+                     const segtaco_sddmm_config *cfg, void *stream);
 
 /* ---- SpMSpV: y = A x, x sparse (nx entries), A given as CSC
  * (col_ptr[K+1], row_idx[nnz], vals) -- the CSR of A^T that segTACO's

@@ -172,10 +172,21 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
       plan->py_entries = 4;  // the two parts' counts, 64-bit work queue
     }
   }
+  plan->window_halo = -1;
+  if ((c.flags & SEGTACO_FLAG_WINDOW) && plan->long_row == 0 && !plan->use_tma && nnz > 0 &&
+      K > 0 &&
+      (schedule == SEGTACO_RB_SR || schedule == SEGTACO_RB_PR) && plan->walk != 2) {
+    // TMA needs B 16-byte aligned and its row pitch a multiple of 16 bytes;
+    // the window's rows (4 per-warp row blocks plus two halos) fit one box.
+    const long long H = c.items_per_unit > 0 ? c.items_per_unit : 32;
+    const long long wrows = 4 * plan->rows_per_unit + 2 * H;
+    if (((uintptr_t)B % 16) == 0 && (ldb * esz) % 16 == 0 && wrows <= 256 &&
+        (size_t)wrows * W * esz <= 60 * 1024 && window_variant_exists(b_dtype, V, G))
+      plan->window_halo = (int)H;
+  }
   if (plan->px_entries)
     plan->workspace = align256((size_t)plan->px_entries * sizeof(int)) +
                       align256((size_t)plan->py_entries * sizeof(int));
-  (void)K;
   return SEGTACO_OK;
 }
 
@@ -209,11 +220,13 @@ int run_spmm_planned(const SpmmPlan &plan, int M, int K, long long nnz, const in
   L.deep = plan.deep;
   L.walk = plan.walk;
   L.no_fork = plan.no_fork;
+  L.window_halo = plan.window_halo;
   const bool bf16 = b_dtype == SEGTACO_BF16;
   switch (plan.schedule) {
     case SEGTACO_RB_SR:
     case SEGTACO_RB_PR:
       if (L.use_tma) return bf16 ? launch_spmm_tma_bf16(L, true, s) : launch_spmm_tma_f32(L, true, s);
+      if (plan.window_halo >= 0) return launch_spmm_window(L, s);
       if (plan.long_row > 0) {
         L.long_row = plan.long_row;
         if (!partition_ready)
@@ -269,6 +282,7 @@ int segtaco_autotune_heuristic(int32_t M, int32_t K, int64_t nnz, int32_t N, int
                                int64_t max_row_len, segtaco_config *cfg) {
   if (!cfg) return set_error(SEGTACO_EINVAL, "cfg is NULL");
   const int requested = cfg->schedule;
+  const bool banded = (cfg->flags & SEGTACO_FLAG_WINDOW) != 0;
   memset(cfg, 0, sizeof(*cfg));
   const double mean = M > 0 ? (double)nnz / M : 0.0;
   // Row-balanced when rows are short and even; merge path otherwise.
@@ -314,6 +328,13 @@ int segtaco_autotune_heuristic(int32_t M, int32_t K, int64_t nnz, int32_t N, int
   // (4.38 ms).
   if (!sequential && esz == 4 && bbytes > 48e6 && N % 8 == 0 && (skewed || nnz >= 4000000))
     cfg->vec = 8;
+  // A B that fits L2 whole (up to ~96 MB) under a large product: one slab of
+  // up to 64 columns (8 per lane, G = 8), so A is read once.  Measured on
+  // GB300, banded 262,144 rows (19.1M nonzeros), N = 64, rb_pr: 0.248 ms
+  // against 0.323 ms with two 32-column slabs.
+  if (!sequential && esz == 4 && bbytes > 48e6 && bbytes <= 96e6 && nnz >= 4000000 &&
+      N % 8 == 0 && !skewed)
+    cfg->col_tile = N < 64 ? N : 64;
   // bf16 likewise: 16 columns per lane (one 32-byte load) on 64-column slabs.
   // Measured on GB300: 1M x 1M power law, N = 128, eb_pr 0.996 -> 0.823 ms;
   // with B in L2 (banded, N = 64) 8 stays faster (0.224 vs 0.235 ms).
@@ -325,6 +346,31 @@ int segtaco_autotune_heuristic(int32_t M, int32_t K, int64_t nnz, int32_t N, int
   cfg->rows_per_unit = schedule == SEGTACO_RB_PR || schedule == SEGTACO_RB_SR ? 4 : 1;
   cfg->depth = (schedule == SEGTACO_RB_SR || schedule == SEGTACO_RB_PR) ? 8 : 4;
   cfg->flags = long_rows ? SEGTACO_FLAG_LONG_ROWS : 0;
+  // Rows known to lie near the diagonal (the caller's segtaco_band_stats):
+  // the staged B window is NOT chosen.  Measured on GB300, banded 262,144
+  // rows, N = 64: the row-block kernel's gathers of the band already hit L1,
+  // and shared-memory reads of the window go through the same load/store
+  // data pipe, so the window (rows_per_unit 16, halo 32) took 0.373 ms fp32
+  // against 0.248 ms for the plain row blocks with one 64-column slab.  The
+  // bit is accepted so that callers may pass their band statistics.
+  (void)banded;
+  return SEGTACO_OK;
+}
+
+int segtaco_spmm_plan_name(int32_t M, int32_t K, int64_t nnz, int32_t N, int32_t b_dtype,
+                           const void *B, int64_t ldb, const segtaco_config *cfg, char *out,
+                           size_t len) {
+  if (!out || len == 0) return set_error(SEGTACO_EINVAL, "out is NULL");
+  SpmmPlan plan;
+  SEGTACO_TRY(plan_spmm(M, K, nnz, N, b_dtype, ldb, N, B, nullptr, cfg, &plan));
+  static const char *sched[] = {"rb_sr", "rb_pr", "eb_sr", "eb_pr"};
+  const char *kernel = plan.use_tma         ? "tma_ring"
+                       : plan.window_halo >= 0 ? "window"
+                       : plan.long_row > 0 ? "long_rows"
+                       : (plan.schedule >= SEGTACO_EB_SR) ? "chunks" : "rows";
+  snprintf(out, len, "%s %s V=%d G=%d W=%d slabs=%d walk=%d halo=%d rows_per_unit=%lld",
+           sched[plan.schedule], kernel, plan.V, plan.G, plan.W, plan.slabs, plan.walk,
+           plan.window_halo, (long long)plan.rows_per_unit);
   return SEGTACO_OK;
 }
 
@@ -483,23 +529,61 @@ int segtaco_spmv(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr, cons
                           s);
 }
 
-int segtaco_sddmm(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr, const int32_t *col,
-                  const float *vals, const void *X, const void *Y, int32_t x_dtype, int64_t ldx,
-                  int64_t ldy, int32_t D, float *out, void *stream) {
+int segtaco_sddmm_autotune(int32_t M, int32_t K, int64_t nnz, int32_t D, int32_t x_dtype,
+                           int64_t max_row_len, segtaco_sddmm_config *cfg) {
+  if (!cfg) return set_error(SEGTACO_EINVAL, "cfg is NULL");
+  if (M < 0 || K < 0 || nnz < 0 || D < 0) return set_error(SEGTACO_EINVAL, "negative size");
+  memset(cfg, 0, sizeof(*cfg));
+  cfg->kernel = SEGTACO_SDDMM_AUTO;
+  // Blocks of 256 nonzeros per warp; smaller for small problems, so that the
+  // launch still holds two waves of warps (152 SMs x 32 warps).
+  const long long two_waves = 2LL * 152 * 32;
+  int blk = 256;
+  while (blk > 32 && (nnz + blk - 1) / blk < two_waves) blk >>= 1;
+  cfg->block_nnz = blk;
+  cfg->lanes = 0;  // from D (sddmm_shape)
+  (void)max_row_len;
+  (void)x_dtype;
+  (void)K;
+  return SEGTACO_OK;
+}
+
+int segtaco_sddmm_ex(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr,
+                     const int32_t *col, const float *vals, const void *X, const void *Y,
+                     int32_t x_dtype, int64_t ldx, int64_t ldy, int32_t D, float *out,
+                     const segtaco_sddmm_config *cfg, void *stream) {
   SEGTACO_TRY(check_csr_args(M, K, nnz, row_ptr, col));
   if (x_dtype != SEGTACO_F32 && x_dtype != SEGTACO_BF16)
     return set_error(SEGTACO_EINVAL, "unknown dense dtype %d", x_dtype);
   if (nnz == 0) return SEGTACO_OK;
   if (D < 0 || ldx < D || ldy < D) return set_error(SEGTACO_EINVAL, "bad D/ldx/ldy");
   if (!X || !Y || !out) return set_error(SEGTACO_EINVAL, "X/Y/out is NULL");
+  segtaco_sddmm_config c;
+  if (cfg)
+    c = *cfg;
+  else
+    SEGTACO_TRY(segtaco_sddmm_autotune(M, K, nnz, D, x_dtype, -1, &c));
+  const long long P = c.block_nnz > 0 ? c.block_nnz : sddmm_block_nnz();
+  if (P < 32 || P > 4096 || (P & (P - 1)))
+    return set_error(SEGTACO_EINVAL, "block_nnz=%lld not a power of two in [32, 4096]", P);
+  if (c.lanes < 0 || c.lanes > 32 || (c.lanes & (c.lanes - 1)))
+    return set_error(SEGTACO_EINVAL, "lanes=%d not 0 or a power of two up to 32", c.lanes);
+  if (c.kernel < SEGTACO_SDDMM_AUTO || c.kernel > SEGTACO_SDDMM_GENERAL)
+    return set_error(SEGTACO_EINVAL, "unknown SDDMM kernel %d", c.kernel);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const long long P = sddmm_block_nnz();
   const long long nblk = (nnz + P - 1) / P;
   Scratch scratch(nullptr, 0, s);
   SEGTACO_TRY(scratch.reserve(align256((size_t)(nblk + 1) * sizeof(int))));
   int *starts = static_cast<int *>(scratch.take((nblk + 1) * sizeof(int)));
   return launch_sddmm(M, nnz, row_ptr, col, vals, X, Y, x_dtype, ldx, ldy, D, out, starts, (int)P,
-                      nblk, s);
+                      nblk, s, false, c.lanes, c.kernel);
+}
+
+int segtaco_sddmm(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr, const int32_t *col,
+                  const float *vals, const void *X, const void *Y, int32_t x_dtype, int64_t ldx,
+                  int64_t ldy, int32_t D, float *out, void *stream) {
+  return segtaco_sddmm_ex(M, K, nnz, row_ptr, col, vals, X, Y, x_dtype, ldx, ldy, D, out, nullptr,
+                          stream);
 }
 
 int segtaco_spmspv(int32_t M, int32_t K, int64_t nnz, const int32_t *col_ptr,

@@ -104,6 +104,59 @@ __device__ __forceinline__ uint32_t ld_u1(const uint16_t *p, uint64_t pol) {
   return r;
 }
 
+// Predicated loads of the dense operand: the destination registers are zeroed
+// and the load runs only where `ok` holds, so a lane with no nonzero to
+// gather moves no data through the load/store pipe (an unpredicated dummy
+// load of a cached row still costs its data-stage wavefronts).
+// PTR, POL and OK name the operand numbers that follow the outputs.
+#define SEGTACO_PRED_LD(TYPE, VEC, OUTS, ZEROS, PTR, POL, OK, ...)                       \
+  asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.b32 q, " OK ", 0;\n\t" ZEROS               \
+               "@q ld.global.nc.L2::cache_hint" VEC "." TYPE " " OUTS ", [" PTR "], " POL   \
+               ";\n\t}"                                                                  \
+               : __VA_ARGS__                                                             \
+               : "l"(p), "l"(pol), "r"((int)ok))
+__device__ __forceinline__ float4 ld_b4_if(const float *p, uint64_t pol, bool ok) {
+  float4 r;
+  SEGTACO_PRED_LD("f32", ".v4", "{%0,%1,%2,%3}",
+                  "mov.b32 %0, 0;\n\tmov.b32 %1, 0;\n\tmov.b32 %2, 0;\n\tmov.b32 %3, 0;\n\t",
+                  "%4", "%5", "%6", "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w));
+  return r;
+}
+__device__ __forceinline__ float2 ld_b2_if(const float *p, uint64_t pol, bool ok) {
+  float2 r;
+  SEGTACO_PRED_LD("f32", ".v2", "{%0,%1}", "mov.b32 %0, 0;\n\tmov.b32 %1, 0;\n\t", "%2", "%3", "%4", "=f"(r.x),
+                  "=f"(r.y));
+  return r;
+}
+__device__ __forceinline__ float ld_b1_if(const float *p, uint64_t pol, bool ok) {
+  float r;
+  SEGTACO_PRED_LD("f32", "", "%0", "mov.b32 %0, 0;\n\t", "%1", "%2", "%3", "=f"(r));
+  return r;
+}
+__device__ __forceinline__ uint4 ld_u4_if(const uint16_t *p, uint64_t pol, bool ok) {
+  uint4 r;
+  SEGTACO_PRED_LD("u32", ".v4", "{%0,%1,%2,%3}",
+                  "mov.b32 %0, 0;\n\tmov.b32 %1, 0;\n\tmov.b32 %2, 0;\n\tmov.b32 %3, 0;\n\t",
+                  "%4", "%5", "%6", "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w));
+  return r;
+}
+__device__ __forceinline__ uint2 ld_u2_if(const uint16_t *p, uint64_t pol, bool ok) {
+  uint2 r;
+  SEGTACO_PRED_LD("u32", ".v2", "{%0,%1}", "mov.b32 %0, 0;\n\tmov.b32 %1, 0;\n\t", "%2", "%3", "%4", "=r"(r.x),
+                  "=r"(r.y));
+  return r;
+}
+__device__ __forceinline__ uint32_t ld_u1_if(const uint16_t *p, uint64_t pol, bool ok) {
+  uint32_t r;
+  SEGTACO_PRED_LD("u32", "", "%0", "mov.b32 %0, 0;\n\t", "%1", "%2", "%3", "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t ld_h1_if(const uint16_t *p, uint64_t pol, bool ok) {
+  uint32_t r;
+  SEGTACO_PRED_LD("u16", "", "%0", "mov.b32 %0, 0;\n\t", "%1", "%2", "%3", "=r"(r));
+  return r;
+}
+
 // bf16 bit pattern -> float (exact: bf16 is the top half of a float).
 __device__ __forceinline__ float bf16lo(uint32_t w) { return __uint_as_float(w << 16); }
 __device__ __forceinline__ float bf16hi(uint32_t w) { return __uint_as_float(w & 0xffff0000u); }
@@ -129,6 +182,22 @@ template <> struct Dense<float, 8> {
                  : "l"(p), "l"(pol));
     return r;
   }
+  static __device__ __forceinline__ raw_t load_if(const float *p, uint64_t pol, bool ok) {
+    F8 r;
+    SEGTACO_PRED_LD("f32", ".v8", "{%0,%1,%2,%3,%4,%5,%6,%7}",
+                    "mov.b32 %0, 0;\n\tmov.b32 %1, 0;\n\tmov.b32 %2, 0;\n\tmov.b32 %3, 0;\n\t"
+                    "mov.b32 %4, 0;\n\tmov.b32 %5, 0;\n\tmov.b32 %6, 0;\n\tmov.b32 %7, 0;\n\t",
+                    "%8", "%9", "%10", "=f"(r.a.x), "=f"(r.a.y), "=f"(r.a.z), "=f"(r.a.w), "=f"(r.b.x), "=f"(r.b.y),
+                    "=f"(r.b.z), "=f"(r.b.w));
+    return r;
+  }
+  // The same slice from shared memory (32-byte aligned).
+  static __device__ __forceinline__ raw_t lds(const float *p) {
+    F8 r;
+    r.a = *reinterpret_cast<const float4 *>(p);
+    r.b = *reinterpret_cast<const float4 *>(p + 4);
+    return r;
+  }
   static __device__ __forceinline__ float get(const raw_t &r, int v) {
     const float4 &h = v < 4 ? r.a : r.b;
     const int w = v & 3;
@@ -140,6 +209,12 @@ template <> struct Dense<float, 4> {
   static __device__ __forceinline__ raw_t load(const float *p, uint64_t pol) {
     return ld_b4<true>(p, pol);
   }
+  static __device__ __forceinline__ raw_t load_if(const float *p, uint64_t pol, bool ok) {
+    return ld_b4_if(p, pol, ok);
+  }
+  static __device__ __forceinline__ raw_t lds(const float *p) {
+    return *reinterpret_cast<const float4 *>(p);
+  }
   static __device__ __forceinline__ float get(const raw_t &r, int v) {
     return v == 0 ? r.x : v == 1 ? r.y : v == 2 ? r.z : r.w;
   }
@@ -149,6 +224,12 @@ template <> struct Dense<float, 2> {
   static __device__ __forceinline__ raw_t load(const float *p, uint64_t pol) {
     return ld_b2<true>(p, pol);
   }
+  static __device__ __forceinline__ raw_t load_if(const float *p, uint64_t pol, bool ok) {
+    return ld_b2_if(p, pol, ok);
+  }
+  static __device__ __forceinline__ raw_t lds(const float *p) {
+    return *reinterpret_cast<const float2 *>(p);
+  }
   static __device__ __forceinline__ float get(const raw_t &r, int v) { return v == 0 ? r.x : r.y; }
 };
 template <> struct Dense<float, 1> {
@@ -156,6 +237,10 @@ template <> struct Dense<float, 1> {
   static __device__ __forceinline__ raw_t load(const float *p, uint64_t pol) {
     return ld_b1<true>(p, pol);
   }
+  static __device__ __forceinline__ raw_t load_if(const float *p, uint64_t pol, bool ok) {
+    return ld_b1_if(p, pol, ok);
+  }
+  static __device__ __forceinline__ raw_t lds(const float *p) { return *p; }
   static __device__ __forceinline__ float get(const raw_t &r, int) { return r; }
 };
 // Sixteen bf16 values in one 32-byte load (ld.global.v8.b32, sm_100+): p is
@@ -173,6 +258,21 @@ template <> struct Dense<uint16_t, 16> {
                  : "l"(p), "l"(pol));
     return r;
   }
+  static __device__ __forceinline__ raw_t load_if(const uint16_t *p, uint64_t pol, bool ok) {
+    U8 r;
+    SEGTACO_PRED_LD("b32", ".v8", "{%0,%1,%2,%3,%4,%5,%6,%7}",
+                    "mov.b32 %0, 0;\n\tmov.b32 %1, 0;\n\tmov.b32 %2, 0;\n\tmov.b32 %3, 0;\n\t"
+                    "mov.b32 %4, 0;\n\tmov.b32 %5, 0;\n\tmov.b32 %6, 0;\n\tmov.b32 %7, 0;\n\t",
+                    "%8", "%9", "%10", "=r"(r.a.x), "=r"(r.a.y), "=r"(r.a.z), "=r"(r.a.w), "=r"(r.b.x), "=r"(r.b.y),
+                    "=r"(r.b.z), "=r"(r.b.w));
+    return r;
+  }
+  static __device__ __forceinline__ raw_t lds(const uint16_t *p) {
+    U8 r;
+    r.a = *reinterpret_cast<const uint4 *>(p);
+    r.b = *reinterpret_cast<const uint4 *>(p + 8);
+    return r;
+  }
   static __device__ __forceinline__ float get(const raw_t &r, int v) {
     const uint4 &h = v < 8 ? r.a : r.b;
     const int q = (v & 7) >> 1;
@@ -185,6 +285,12 @@ template <> struct Dense<uint16_t, 8> {
   static __device__ __forceinline__ raw_t load(const uint16_t *p, uint64_t pol) {
     return ld_u4<true>(p, pol);
   }
+  static __device__ __forceinline__ raw_t load_if(const uint16_t *p, uint64_t pol, bool ok) {
+    return ld_u4_if(p, pol, ok);
+  }
+  static __device__ __forceinline__ raw_t lds(const uint16_t *p) {
+    return *reinterpret_cast<const uint4 *>(p);
+  }
   static __device__ __forceinline__ float get(const raw_t &r, int v) {
     const uint32_t w = v < 2 ? r.x : v < 4 ? r.y : v < 6 ? r.z : r.w;
     return (v & 1) ? bf16hi(w) : bf16lo(w);
@@ -194,6 +300,12 @@ template <> struct Dense<uint16_t, 4> {
   using raw_t = uint2;
   static __device__ __forceinline__ raw_t load(const uint16_t *p, uint64_t pol) {
     return ld_u2<true>(p, pol);
+  }
+  static __device__ __forceinline__ raw_t load_if(const uint16_t *p, uint64_t pol, bool ok) {
+    return ld_u2_if(p, pol, ok);
+  }
+  static __device__ __forceinline__ raw_t lds(const uint16_t *p) {
+    return *reinterpret_cast<const uint2 *>(p);
   }
   static __device__ __forceinline__ float get(const raw_t &r, int v) {
     const uint32_t w = v < 2 ? r.x : r.y;
@@ -205,6 +317,12 @@ template <> struct Dense<uint16_t, 2> {
   static __device__ __forceinline__ raw_t load(const uint16_t *p, uint64_t pol) {
     return ld_u1<true>(p, pol);
   }
+  static __device__ __forceinline__ raw_t load_if(const uint16_t *p, uint64_t pol, bool ok) {
+    return ld_u1_if(p, pol, ok);
+  }
+  static __device__ __forceinline__ raw_t lds(const uint16_t *p) {
+    return *reinterpret_cast<const uint32_t *>(p);
+  }
   static __device__ __forceinline__ float get(const raw_t &r, int v) {
     return (v & 1) ? bf16hi(r) : bf16lo(r);
   }
@@ -213,6 +331,12 @@ template <> struct Dense<uint16_t, 1> {
   using raw_t = uint32_t;
   static __device__ __forceinline__ raw_t load(const uint16_t *p, uint64_t) {
     return (uint32_t)__ldg(reinterpret_cast<const unsigned short *>(p));
+  }
+  static __device__ __forceinline__ raw_t load_if(const uint16_t *p, uint64_t pol, bool ok) {
+    return ld_h1_if(p, pol, ok);
+  }
+  static __device__ __forceinline__ raw_t lds(const uint16_t *p) {
+    return (uint32_t)*p;
   }
   static __device__ __forceinline__ float get(const raw_t &r, int) { return bf16lo(r); }
 };

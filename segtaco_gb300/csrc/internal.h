@@ -79,6 +79,8 @@ struct SpmmLaunch {
   int carveout = -1;           // >= 0: preferred shared-memory carveout (%) of the launch
   bool no_fork = false;        // rb long rows: both kernels on the call's stream (no side
                                // stream or events are created)
+  int window_halo = -1;        // >= 0: rb rows with B rows [i0 - halo, i1 + halo) of each
+                               // row block staged by TMA (spmm_window.cu)
 };
 // One launcher per (dense type, unit kind); each switches over (V, G).
 int launch_spmm_f32_rows(const SpmmLaunch &L, cudaStream_t s);
@@ -90,6 +92,11 @@ int launch_spmm_tma_f32(const SpmmLaunch &L, bool rows, cudaStream_t s);
 int launch_spmm_tma_bf16(const SpmmLaunch &L, bool rows, cudaStream_t s);
 // Device status word of the TMA kernels on the current device.
 int tma_status_ptr(int **out);
+// Row blocks with their B window staged in shared memory (rb only).
+int launch_spmm_window(const SpmmLaunch &L, cudaStream_t s);
+bool window_variant_exists(int dtype, int V, int G);
+int launch_band_stats(const int *row_ptr, const int *col, int M, int K, int halo,
+                      unsigned long long *out, cudaStream_t s);
 
 // Resolved plan of one SpMM call (api.cu).
 struct SpmmPlan {
@@ -104,6 +111,7 @@ struct SpmmPlan {
   int walk;                  // kWalkRows / kWalkRowsDeep / kWalkFlat
   int long_row;              // rb: long-row threshold (0: every row in the row-block kernel)
   bool no_fork = false;      // rb long rows: no side stream (segtaco_spmm_noalloc)
+  int window_halo = -1;      // rb: >= 0 stages each row block's B window (spmm_window.cu)
   long long px_entries;      // int32 entries of the first workspace array (eb: chunk-edge
                              // rows; rb long rows: the list of long rows)
   long long py_entries;      // ... of the second (eb: chunk-edge nonzeros; long rows: counters)
@@ -138,7 +146,7 @@ struct SddmmShape {
   int family = 0, KI = 0, G = 0, V = 1;
 };
 SddmmShape sddmm_shape(int x_dtype, int D, long long ldx, long long ldy, const void *X,
-                       const void *Y);
+                       const void *Y, int lanes = 0);
 // One launch over `nprobs` problems of the fixed shape `sh` (device array
 // `probs`, blocks 0 .. total_blocks - 1); their block starts must be ready.
 int launch_sddmm_multi(const SddmmShape &sh, int x_dtype, const SddmmProblem *probs, int nprobs,
@@ -148,7 +156,8 @@ int launch_sddmm_multi(const SddmmShape &sh, int x_dtype, const SddmmProblem *pr
 int launch_sddmm(int M, long long nnz, const int *row_ptr, const int *col, const float *val,
                  const void *X, const void *Y, int x_dtype, long long ldx, long long ldy, int D,
                  float *out, int *starts, int P, long long nblk, cudaStream_t s,
-                 bool starts_ready = false);
+                 bool starts_ready = false, int lanes = 0,
+                 int kernel = 0);
 // ---- long rows of the row-block schedules (spmm_long.cu) ----
 // Row-block products below this many nonzeros walk every row in the row-block
 // kernel: the list pass and the fork would cost more than a long row there.

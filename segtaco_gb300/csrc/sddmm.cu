@@ -27,15 +27,15 @@ __global__ void __launch_bounds__(kCta, 3) sddmm_kernel(int M, long long nnz,
                                                     const XT *__restrict__ Y, long long ldx,
                                                     long long ldy, int D, float *__restrict__ out,
                                                     const int *__restrict__ starts,
-                                                    long long nblk) {
+                                                    long long nblk, int blk) {
   constexpr int P = 32 / G;  // nonzeros per step
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int g = lane / G, gl = lane & (G - 1);
   const long long w = (long long)blockIdx.x * (kCta / 32) + threadIdx.x / 32;
   if (w >= nblk) return;
-  const long long pb = w * kSddmmBlock;
-  const long long pe = pb + kSddmmBlock < nnz ? pb + kSddmmBlock : nnz;
+  const long long pb = w * blk;
+  const long long pe = pb + blk < nnz ? pb + blk : nnz;
   int wb = __ldg(starts + w);  // row of nonzero pb
   int rw = (wb + lane < M) ? __ldg(row_ptr + wb + 1 + lane) : INT_MAX;
   for (long long p = pb; p < pe; p += 32) {
@@ -130,15 +130,15 @@ __device__ __forceinline__ void sddmm_fixed_block(
     int M, long long nnz, const int *__restrict__ row_ptr, const int *__restrict__ col,
     const float *__restrict__ val, const XT *__restrict__ X, const XT *__restrict__ Y,
     long long ldx, long long ldy, float *__restrict__ out, const int *__restrict__ starts,
-    long long w) {
+    long long w, int blk) {
   constexpr int P = 32 / G;
   using Dv = Dense<XT, V>;
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int g = lane / G, gl = lane & (G - 1);
   const uint64_t pol = l2_policy_evict_normal();
-  const long long pb = w * kSddmmBlock;
-  const long long pe = pb + kSddmmBlock < nnz ? pb + kSddmmBlock : nnz;
+  const long long pb = w * blk;
+  const long long pe = pb + blk < nnz ? pb + blk : nnz;
   int wb = __ldg(starts + w);  // row of nonzero pb
   int rw = (wb + lane < M) ? __ldg(row_ptr + wb + 1 + lane) : INT_MAX;
   // The group's slice of X[xrow] stays in registers while its nonzeros stay in
@@ -215,10 +215,11 @@ __global__ void __launch_bounds__(kCta, 4) sddmm_fixed_kernel(
     int M, long long nnz, const int *__restrict__ row_ptr, const int *__restrict__ col,
     const float *__restrict__ val, const XT *__restrict__ X, const XT *__restrict__ Y,
     long long ldx, long long ldy, float *__restrict__ out, const int *__restrict__ starts,
-    long long nblk) {
+    long long nblk, int blk) {
   const long long w = (long long)blockIdx.x * (kCta / 32) + threadIdx.x / 32;
   if (w >= nblk) return;  // whole warp leaves together
-  sddmm_fixed_block<XT, V, G, KI>(M, nnz, row_ptr, col, val, X, Y, ldx, ldy, out, starts, w);
+  sddmm_fixed_block<XT, V, G, KI>(M, nnz, row_ptr, col, val, X, Y, ldx, ldy, out, starts, w,
+                                  blk);
 }
 
 // Several problems of one shape in one launch: warp w takes block
@@ -239,11 +240,12 @@ __global__ void __launch_bounds__(kCta, 4) sddmm_fixed_multi_kernel(
   const SddmmProblem &a = probs[lo];
   sddmm_fixed_block<XT, V, G, KI>(a.M, a.nnz, a.row_ptr, a.col, a.val,
                                   static_cast<const XT *>(a.X), static_cast<const XT *>(a.Y),
-                                  a.ldx, a.ldy, a.out, a.starts, w - a.blk_begin);
+                                  a.ldx, a.ldy, a.out, a.starts, w - a.blk_begin, kSddmmBlock);
 }
 
 // Fixed shapes (KI, G) of each family, for both launches.
-#define SEGTACO_SDDMM_SHAPES32(X_) X_(1, 1) X_(1, 2) X_(1, 4) X_(2, 4) X_(2, 8) X_(2, 16)
+#define SEGTACO_SDDMM_SHAPES32(X_) \
+  X_(1, 1) X_(1, 2) X_(1, 4) X_(2, 4) X_(2, 8) X_(2, 16) X_(1, 8) X_(1, 16) X_(1, 32)
 #define SEGTACO_SDDMM_SHAPES16(X_) \
   X_(1, 1) X_(2, 1) X_(4, 1) X_(4, 2) X_(4, 4) X_(4, 8) X_(4, 16) X_(4, 32)
 
@@ -251,7 +253,7 @@ __global__ void __launch_bounds__(kCta, 4) sddmm_fixed_multi_kernel(
 // family 1 = fp32 32-byte lanes (V = 8), 2 = bf16 32-byte lanes (V = 16),
 // 3 = 16-byte lanes (V = 16 / element size), 0 = the general kernel.
 SddmmShape sddmm_shape(int x_dtype, int D, long long ldx, long long ldy, const void *X,
-                       const void *Y) {
+                       const void *Y, int lanes) {
   SddmmShape sh;
   const int esz = x_dtype == SEGTACO_BF16 ? 2 : 4;
   const uintptr_t al = (uintptr_t)X | (uintptr_t)Y;
@@ -268,6 +270,11 @@ SddmmShape sddmm_shape(int x_dtype, int D, long long ldx, long long ldy, const v
     if (T >= 1 && T <= 32 && (T & (T - 1)) == 0) {
       sh.family = esz == 4 ? 1 : 2;
       sh.G = T < 4 ? T : (T / 2 > 4 ? T / 2 : 4);
+      // A requested lane count with one load per lane, or two from 4 lanes
+      // (the compiled shapes); other requests keep the default.
+      if (lanes > 0 && (lanes & (lanes - 1)) == 0 && T % lanes == 0 &&
+          (T / lanes == 1 || (T / lanes == 2 && lanes >= 4)))
+        sh.G = lanes;
       sh.KI = T / sh.G;
       return sh;
     }
@@ -278,6 +285,10 @@ SddmmShape sddmm_shape(int x_dtype, int D, long long ldx, long long ldy, const v
     if (T >= 1 && T <= 128 && (T & (T - 1)) == 0) {
       sh.family = 3;
       sh.KI = T < 4 ? T : 4;
+      // A requested lane count with four loads per lane (the compiled
+      // shapes); other requests keep the default.
+      if (lanes > 0 && (lanes & (lanes - 1)) == 0 && T >= 4 && T % lanes == 0 && T / lanes == 4)
+        sh.KI = 4;
       sh.G = T / sh.KI;
     }
   }
@@ -285,11 +296,6 @@ SddmmShape sddmm_shape(int x_dtype, int D, long long ldx, long long ldy, const v
 }
 
 namespace {
-
-// Fixed shapes (KI, G) of each family.
-#define SEGTACO_SDDMM_SHAPES32(X_) X_(1, 1) X_(1, 2) X_(1, 4) X_(2, 4) X_(2, 8) X_(2, 16)
-#define SEGTACO_SDDMM_SHAPES16(X_) \
-  X_(1, 1) X_(2, 1) X_(4, 1) X_(4, 2) X_(4, 4) X_(4, 8) X_(4, 16) X_(4, 32)
 // Switch over the family's shapes, each case launching CASE_(XT, V, KI, G).
 #define SEGTACO_SDDMM_SWITCH(sh, x_dtype)                                                  \
   switch ((sh).family * 10000 + (sh).KI * 100 + (sh).G) {                                \
@@ -321,12 +327,12 @@ namespace {
 int launch_fixed_single(const SddmmShape &sh, int x_dtype, dim3 grid, int M, long long nnz,
                         const int *row_ptr, const int *col, const float *val, const void *X,
                         const void *Y, long long ldx, long long ldy, float *out, const int *starts,
-                        long long nblk, cudaStream_t s) {
+                        long long nblk, int blk, cudaStream_t s) {
 #define CASE_(XT, V, KI, G)                                                                \
   sddmm_fixed_kernel<XT, V, G, KI><<<grid, kCta, 0, s>>>(M, nnz, row_ptr, col, val,       \
                                                          static_cast<const XT *>(X),      \
                                                          static_cast<const XT *>(Y), ldx, \
-                                                         ldy, out, starts, nblk);
+                                                         ldy, out, starts, nblk, blk);
   SEGTACO_SDDMM_SWITCH(sh, x_dtype)
 #undef CASE_
   return check_launch("sddmm_fixed_kernel");
@@ -348,24 +354,24 @@ int launch_fixed_multi(const SddmmShape &sh, int x_dtype, dim3 grid, const Sddmm
     sddmm_kernel<XT, V, G><<<grid, kCta, 0, s>>>(M, nnz, row_ptr, col, val,                   \
                                                  static_cast<const XT *>(X),                  \
                                                  static_cast<const XT *>(Y), ldx, ldy, D, out, \
-                                                 starts, nblk);                               \
+                                                 starts, nblk, P);                            \
     break;
 
 int launch_sddmm(int M, long long nnz, const int *row_ptr, const int *col, const float *val,
                  const void *X, const void *Y, int x_dtype, long long ldx, long long ldy, int D,
                  float *out, int *starts, int P, long long nblk, cudaStream_t s,
-                 bool starts_ready) {
+                 bool starts_ready, int lanes, int kernel) {
   if (nnz == 0) return SEGTACO_OK;
-  (void)P;
   if (!starts_ready)
-    SEGTACO_TRY(launch_block_starts_canonical(row_ptr, M, kSddmmBlock, nblk, starts, s));
+    SEGTACO_TRY(launch_block_starts_canonical(row_ptr, M, P, nblk, starts, s));
   const dim3 grid((unsigned)((nblk + (kCta / 32) - 1) / (kCta / 32)));
-  // The fixed-shape kernel where D and the operands allow it; the general
-  // kernel (V-wide vectors, G lanes covering D) otherwise.
-  const SddmmShape sh = sddmm_shape(x_dtype, D, ldx, ldy, X, Y);
-  if (sh.family != 0)
+  // The fixed-shape kernel where D and the operands allow it (unless the
+  // general one is asked for); the general kernel (V-wide vectors, G lanes
+  // covering D) otherwise.
+  const SddmmShape sh = sddmm_shape(x_dtype, D, ldx, ldy, X, Y, lanes);
+  if (sh.family != 0 && kernel != SEGTACO_SDDMM_GENERAL)
     return launch_fixed_single(sh, x_dtype, grid, M, nnz, row_ptr, col, val, X, Y, ldx, ldy, out,
-                               starts, nblk, s);
+                               starts, nblk, P, s);
   const int V = sh.V;
   // Lanes per dot product: enough to cover D in one pass, at most 32.
   int G = 1;

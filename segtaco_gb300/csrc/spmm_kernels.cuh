@@ -83,11 +83,83 @@ template <int G, int V> __device__ __forceinline__ void fold_slots(float (&r)[V]
   }
 }
 
+// Reduce-scatter form of fold_slots: at each xor level the lane keeps one half
+// of its remaining values and trades the other half with its partner, so the
+// P slots' sums end spread over the lanes (P = 8, V = 8: 7 shuffles instead of
+// 24, one column per lane).  On return the lane holds the sums of its columns
+// col0 + first .. col0 + first + R - 1 in r[0 .. R-1], R = fold_scatter_count.
+// Where the values run out before the slots do (V < P), the last levels add
+// whole values and only the lanes with a clear bit at those levels own the
+// result (`owner`), so that each column is written once.
+template <int G, int V> __host__ __device__ constexpr int fold_scatter_count() {
+  int c = V;
+  for (int o = G; o < 32; o <<= 1)
+    if (c >= 2) c /= 2;
+  return c;
+}
+template <int G, int V>
+__device__ __forceinline__ int fold_slots_scatter(float (&r)[V], int lane, bool &owner) {
+  int first = 0;
+  int c = V;
+  owner = true;
+#pragma unroll
+  for (int o = G; o < 32; o <<= 1) {
+    const bool hi = (lane & o) != 0;
+    if (c >= 2) {
+      const int h = c / 2;
+#pragma unroll
+      for (int i = 0; i < V / 2; ++i) {
+        if (i < h) {
+          const float keep = hi ? r[i + h] : r[i];
+          const float send = hi ? r[i] : r[i + h];
+          r[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+      }
+      if (hi) first += h;
+      c = h;
+    } else {
+      r[0] += __shfl_xor_sync(0xffffffffu, r[0], o);
+      if (hi) owner = false;
+    }
+  }
+  return first;
+}
+
+// Store (or, at partition edges, add) R consecutive floats.
+template <int R> __device__ __forceinline__ void put_c(float *p, const float *a, bool add) {
+  if constexpr (R >= 4) {
+#pragma unroll
+    for (int k = 0; k < R; k += 4) {
+      if (add)
+        red_add4(p + k, a[k], a[k + 1], a[k + 2], a[k + 3]);
+      else
+        __stcs(reinterpret_cast<float4 *>(p + k), make_float4(a[k], a[k + 1], a[k + 2], a[k + 3]));
+    }
+  } else if constexpr (R == 2) {
+    if (add)
+      red_add2(p, a[0], a[1]);
+    else
+      __stcs(reinterpret_cast<float2 *>(p), make_float2(a[0], a[1]));
+  } else {
+    if (add)
+      atomicAdd(p, a[0]);
+    else
+      __stcs(p, a[0]);
+  }
+}
+
+// Rows [lo, lo + rows) of the current column slab of B staged in shared
+// memory (W = G*V values per row): gathers of those rows read the copy.
+template <typename BT> struct Window {
+  const BT *base = nullptr;
+  int lo = 0, rows = 0;
+};
+
 // Walk one unit (merge-path chunk or row block) `w` over column slab `slab`.
 // The body of every SpMM kernel below (single problem or batched).
-template <typename BT, int V, int G, bool ROWS, bool DEEP>
+template <typename BT, int V, int G, bool ROWS, bool DEEP, bool WIN = false>
 __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long w, int slab,
-                                               int lane) {
+                                               int lane, Window<BT> win = Window<BT>()) {
   constexpr int P = 32 / G;                 // slots
   // Rows with >= LONG nonzeros are split over the slots (LONG <= 32, so a
   // short row always fits one batch).
@@ -106,6 +178,14 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
   // out of bounds; their results are never stored.
   const BT *Bc = a.B + (active ? col0 : 0);
   const unsigned ldb = (unsigned)a.ldb;
+  // B row slice j of this lane: from the staged window when it holds row j.
+  auto gather = [&](int j) -> typename D::raw_t {
+    if constexpr (WIN) {
+      const unsigned d = (unsigned)(j - win.lo);
+      if (d < (unsigned)win.rows) return D::lds(win.base + d * (G * V) + gl * V);
+    }
+    return D::load(Bc + (size_t)(unsigned)j * ldb, pol);
+  };
 
   int x0, x1, y0, y1;
   bool head_split = false, tail_open = false;
@@ -180,7 +260,7 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
             }
             typename D::raw_t bb[R];
 #pragma unroll
-            for (int b = 0; b < R; ++b) bb[b] = D::load(Bc + (size_t)(unsigned)jc[b] * ldb, pol);
+            for (int b = 0; b < R; ++b) bb[b] = gather(jc[b]);
 #pragma unroll
             for (int b = 0; b < R; ++b) {
 #pragma unroll
@@ -213,7 +293,7 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
               const int t = (s0 + u) * P + slot;
               const int j = __shfl_sync(FULL, mc, t);
               vv[u] = __shfl_sync(FULL, mv, t);
-              b[u] = D::load(Bc + (size_t)(unsigned)j * ldb, pol);
+              b[u] = gather(j);
             }
 #pragma unroll
             for (int u = 0; u < UB; ++u) {
@@ -232,7 +312,7 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
               const int j = __shfl_sync(FULL, mc, ok ? t : 0);
               const float v = __shfl_sync(FULL, mv, ok ? t : 0);
               vv[u] = ok ? v : 0.0f;
-              b[u] = D::load(Bc + (size_t)(unsigned)j * ldb, pol);
+              b[u] = gather(j);
             }
 #pragma unroll
             for (int u = 0; u < UB; ++u) {
@@ -246,8 +326,17 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
         mc = mcn;
         mv = mvn;
       }
-      fold_slots<G, V>(acc);
-      if (slot == 0 && active) {
+      if constexpr (P > 1) {
+        // the slots' sums, spread over the lanes: every lane writes its share
+        bool owner;
+        const int first = fold_slots_scatter<G, V>(acc, lane, owner);
+        if (active && owner) {
+          const bool edge = !ROWS && ((cur == x0 && head_split) || (cur == x1 && tail_open));
+          constexpr int R = fold_scatter_count<G, V>();
+          put_c<R>(a.C + (long long)cur * a.ldc + col0 + first, acc,
+                                            edge);
+        }
+      } else if (active) {
         float *dst = a.C + (long long)cur * a.ldc + col0;
         if (!ROWS && ((cur == x0 && head_split) || (cur == x1 && tail_open)))
           atomic_add_c<V>(dst, acc);
@@ -292,7 +381,7 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
           const int j = __shfl_sync(FULL, mc, t);
           const float v = __shfl_sync(FULL, mv, t);
           vv[u] = okk ? v : 0.0f;
-          b[u] = D::load(Bc + (size_t)(unsigned)j * ldb, pol);
+          b[u] = gather(j);
         }
 #pragma unroll
         for (int u = 0; u < UL; ++u) {

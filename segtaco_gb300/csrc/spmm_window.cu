@@ -1,0 +1,248 @@
+// spmm_window.cu -- row-block SpMM with the reused B rows staged by TMA.
+//
+// For matrices whose nonzeros cluster around the diagonal (banded, block
+// diagonal, meshes), the rows of a row block gather B rows from a short range
+// around the block: rows i0 .. i1-1 touch B rows near [i0 - H, i1 + H).  Each
+// 128-thread CTA here owns a block of 4 * rows_per_unit rows and one column
+// slab; one thread brings the window B[i0 - H .. i1 + H) x slab into shared
+// memory with a single cp.async.bulk.tensor.2d copy (a tensor map over B,
+// box = window rows x slab columns; rows outside [0, K) are zero-filled by the
+// copy engine), completing on an mbarrier.  Then the four warps walk their row
+// blocks exactly as the row-block kernel does (spmm_walk_unit), except that a
+// gather of a B row inside the window reads the shared copy; rows outside it
+// (the off-band nonzeros) are still gathered from global memory.  So every
+// in-band B row crosses L2 once per row block instead of once per nonzero.
+//
+// The wait is bounded: after kWindowSpin polls the CTA records SEGTACO_ETIMEOUT
+// in the device status word (segtaco_device_status), waits once more, bounded,
+// for its copy, and leaves its rows unwritten.
+//
+// Same results as the row-block kernel: the walk, its summation order and its
+// stores are unchanged, only where a B value is read from.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <atomic>
+#include <mutex>
+
+#include "spmm_launch.cuh"
+
+namespace segtaco {
+namespace {
+
+constexpr long long kWindowSpin = 1LL << 22;
+
+__device__ __forceinline__ uint32_t sm_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ bool window_wait(uint32_t bar) {
+  for (long long i = 0; i < kWindowSpin; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(bar), "r"(0)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// Most gathers come from shared memory here, so fewer resident warps hide
+// the latency: 16 warps per SM, whose registers hold the walk and both
+// gather paths without spilling.
+template <typename BT, int V, int G> constexpr int window_min_ctas() {
+  return 16 / kSpmmWarps;
+}
+
+template <typename BT, int V, int G>
+__global__ void __launch_bounds__(kSpmmCta, window_min_ctas<BT, V, G>())
+    spmm_window_kernel(SpmmArgs<BT> a, const __grid_constant__ CUtensorMap tm, int halo,
+                       int *status) {
+  constexpr int W = G * V;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const long long rows_blk = (long long)kSpmmWarps * a.rows_per_unit;
+  const int wrows = (int)(rows_blk + 2 * halo);
+  BT *win = reinterpret_cast<BT *>(smem);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + (((size_t)wrows * W * sizeof(BT) + 15) & ~size_t(15)));
+  const int wlo = (int)((long long)blockIdx.x * rows_blk - halo);
+  const uint32_t b = sm_u32(bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t bytes = (uint32_t)((size_t)wrows * W * sizeof(BT));
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes)
+                 : "memory");
+    // x = the slab's first column (a multiple of W: 16-byte aligned), y = the
+    // window's first row (negative at the top edge: zero-filled)
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cta.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(sm_u32(win)),
+        "l"(&tm), "r"((int)(blockIdx.y * W)), "r"(wlo), "r"(b)
+        : "memory");
+  }
+  if (!window_wait(b)) {
+    if (threadIdx.x == 0) atomicExch(status, SEGTACO_ETIMEOUT);
+    window_wait(b);  // the copy may still land: wait for it once more, bounded
+    return;
+  }
+  const long long w = (long long)blockIdx.x * kSpmmWarps + threadIdx.x / 32;
+  if (w >= a.units) return;
+  Window<BT> wv;
+  wv.base = win;
+  wv.lo = wlo;
+  wv.rows = wrows;
+  spmm_walk_unit<BT, V, G, true, false, true>(a, w, blockIdx.y, threadIdx.x & 31, wv);
+}
+
+// cuTensorMapEncodeTiled from the driver, looked up once.
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static std::once_flag once;
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+template <typename BT, int V, int G> int launch_window_variant(const SpmmLaunch &L, cudaStream_t s) {
+  constexpr int W = G * V;
+  const long long rows_blk = (long long)kSpmmWarps * L.rows_per_unit;
+  const long long wrows = rows_blk + 2LL * L.window_halo;
+  if (wrows > 256)
+    return set_error(SEGTACO_EINVAL, "window of %lld rows (4*rows_per_unit + 2*halo) > 256",
+                     wrows);
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return set_error(SEGTACO_EUNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
+  CUtensorMap tm;
+  const cuuint64_t dims[2] = {(cuuint64_t)L.N, (cuuint64_t)L.K};
+  const cuuint64_t strides[1] = {(cuuint64_t)L.ldb * sizeof(BT)};
+  const cuuint32_t box[2] = {(cuuint32_t)W, (cuuint32_t)wrows};
+  const cuuint32_t es[2] = {1, 1};
+  const CUresult r = enc(&tm, sizeof(BT) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                               : CU_TENSOR_MAP_DATA_TYPE_UINT16,
+                         2, const_cast<void *>(L.B), dims, strides, box, es,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    return set_error(SEGTACO_EINVAL, "window: tensor map of B rejected (CUresult %d)", (int)r);
+  const size_t bytes = (((size_t)wrows * W * sizeof(BT) + 15) & ~size_t(15)) + 16;
+  auto kern = spmm_window_kernel<BT, V, G>;
+  // The shared-memory opt-in, once per device.
+  static std::atomic<unsigned long long> opted{0};
+  int dev = 0;
+  SEGTACO_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (!(opted.load() & bit)) {
+    SEGTACO_TRY(check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)(64 * 1024)),
+                           "cudaFuncSetAttribute(spmm_window_kernel)"));
+    opted.fetch_or(bit);
+  }
+  if (bytes > 64 * 1024) return set_error(SEGTACO_EINVAL, "window of %zu bytes > 64 KB", bytes);
+  int *status = nullptr;
+  SEGTACO_TRY(tma_status_ptr(&status));
+  const SpmmArgs<BT> a = make_spmm_args<BT>(L);
+  const dim3 grid = spmm_grid(L);
+  kern<<<grid, kSpmmCta, bytes, s>>>(a, tm, L.window_halo, status);
+  return check_launch("spmm_window_kernel");
+}
+
+template <typename BT> int launch_window(const SpmmLaunch &L, cudaStream_t s) {
+  switch (L.V * 100 + L.G) {
+#define SEGTACO_WINDOW_CASE(V, G) \
+  case V * 100 + G:               \
+    return launch_window_variant<BT, V, G>(L, s);
+    SEGTACO_WINDOW_CASE(8, 4)
+    SEGTACO_WINDOW_CASE(4, 8)
+    SEGTACO_WINDOW_CASE(8, 8)
+    SEGTACO_WINDOW_CASE(4, 16)
+    SEGTACO_WINDOW_CASE(8, 16)
+    SEGTACO_WINDOW_CASE(1, 32)
+    SEGTACO_WINDOW_CASE(2, 32)
+#undef SEGTACO_WINDOW_CASE
+    default:
+      break;
+  }
+  if constexpr (sizeof(BT) == 2) {
+    if (L.V == 16 && L.G == 4) return launch_window_variant<BT, 16, 4>(L, s);
+  }
+  return set_error(SEGTACO_EUNSUPPORTED, "window: no variant V=%d G=%d", L.V, L.G);
+}
+
+// Nonzeros within `halo` of the diagonal (row i scaled to column i*K/M).
+__global__ void band_stats_kernel(const int *__restrict__ row_ptr, const int *__restrict__ col,
+                                  int M, int K, int halo, unsigned long long *out) {
+  unsigned long long n = 0;
+  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < M;
+       r += (long long)gridDim.x * blockDim.x) {
+    const long long d = M > 0 ? r * K / M : 0;
+    const int p1 = __ldg(row_ptr + r + 1);
+    for (int p = __ldg(row_ptr + r); p < p1; ++p) {
+      const long long c = __ldg(col + p);
+      n += (c >= d - halo && c <= d + halo) ? 1 : 0;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+  if ((threadIdx.x & 31) == 0 && n) atomicAdd(out, n);
+}
+
+}  // namespace
+
+int launch_band_stats(const int *row_ptr, const int *col, int M, int K, int halo,
+                      unsigned long long *out, cudaStream_t s) {
+  SEGTACO_TRY(check_cuda(cudaMemsetAsync(out, 0, sizeof(unsigned long long), s), "memset"));
+  if (M <= 0) return SEGTACO_OK;
+  long long blocks = (M + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  band_stats_kernel<<<(unsigned)blocks, 256, 0, s>>>(row_ptr, col, M, K, halo, out);
+  return check_launch("band_stats_kernel");
+}
+
+bool window_variant_exists(int dtype, int V, int G) {
+  const int k = V * 100 + G;
+  if (k == 804 || k == 408 || k == 808 || k == 416 || k == 816 || k == 132 || k == 232)
+    return true;
+  return dtype == SEGTACO_BF16 && k == 1604;
+}
+
+int launch_spmm_window(const SpmmLaunch &L, cudaStream_t s) {
+  return L.dtype == SEGTACO_BF16 ? launch_window<uint16_t>(L, s) : launch_window<float>(L, s);
+}
+
+}  // namespace segtaco
+
+using namespace segtaco;
+
+extern "C" int segtaco_band_stats(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr,
+                                  const int32_t *col, int32_t halo, int64_t *in_band,
+                                  void *stream) {
+  if (M < 0 || K < 0 || nnz < 0 || halo < 0 || !in_band)
+    return set_error(SEGTACO_EINVAL, "segtaco_band_stats: bad arguments");
+  *in_band = 0;
+  if (M == 0 || nnz == 0) return SEGTACO_OK;
+  if (!row_ptr || !col) return set_error(SEGTACO_EINVAL, "segtaco_band_stats: NULL CSR");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Scratch scratch(nullptr, 0, s);
+  SEGTACO_TRY(scratch.reserve(256));
+  auto *d = static_cast<unsigned long long *>(scratch.take(sizeof(unsigned long long)));
+  SEGTACO_TRY(launch_band_stats(row_ptr, col, M, K, halo, d, s));
+  unsigned long long h = 0;
+  SEGTACO_TRY(check_cuda(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, s), "copy"));
+  SEGTACO_TRY(check_cuda(cudaStreamSynchronize(s), "sync"));
+  *in_band = (int64_t)h;
+  return SEGTACO_OK;
+}

@@ -38,6 +38,7 @@ FLAG_TMA_BULK = 8
 FLAG_ROW_WALK = 16
 FLAG_FLAT_WALK = 32
 FLAG_LONG_ROWS = 64
+FLAG_WINDOW = 128
 
 
 class SegtacoError(RuntimeError):
@@ -61,6 +62,22 @@ class Config(C.Structure):
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class SddmmConfig(C.Structure):
+    """segtaco_sddmm_config: kernel, nonzeros per warp block, lanes per dot product."""
+    _fields_ = [("kernel", C.c_int32), ("block_nnz", C.c_int32), ("lanes", C.c_int32),
+                ("reserved", C.c_int32)]
+
+    @classmethod
+    def make(cls, kernel=0, block_nnz=0, lanes=0):
+        return cls(kernel, block_nnz, lanes, 0)
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+SDDMM_AUTO, SDDMM_FIXED, SDDMM_GENERAL = 0, 1, 2
 
 
 class SpmmProblem(C.Structure):
@@ -147,6 +164,9 @@ SIGNATURES = {
     "segtaco_batch_info": (C.c_int, [_P, C.POINTER(_I), C.POINTER(_I64), C.POINTER(Config)]),
     "segtaco_batch_destroy": (C.c_int, [_P]),
     "segtaco_row_stats": (C.c_int, [_I, _P, C.POINTER(_I64), _P]),
+    "segtaco_band_stats": (C.c_int, [_I, _I, _I64, _P, _P, _I, C.POINTER(_I64), _P]),
+    "segtaco_spmm_plan_name": (C.c_int, [_I, _I, _I64, _I, _I, _P, _I64, _P, C.c_char_p,
+                                         C.c_size_t]),
     "segtaco_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(_P)]),
     "segtaco_server_add_matrix": (C.c_int, [_P, _I64, _I, _I, _I64, _P, _P, _P]),
     "segtaco_server_submit": (C.c_int, [_P, C.POINTER(Request), C.POINTER(_I64)]),
@@ -169,6 +189,9 @@ SIGNATURES = {
     "segtaco_spmv_workspace_size": (C.c_int, [_I, _I64, C.POINTER(_SZ)]),
     "segtaco_spmv": (C.c_int, [_I, _I, _I64, _P, _P, _P, _P, _P, _P, _SZ, _P]),
     "segtaco_sddmm": (C.c_int, [_I, _I, _I64, _P, _P, _P, _P, _P, _I, _I64, _I64, _I, _P, _P]),
+    "segtaco_sddmm_autotune": (C.c_int, [_I, _I, _I64, _I, _I, _I64, C.POINTER(SddmmConfig)]),
+    "segtaco_sddmm_ex": (C.c_int, [_I, _I, _I64, _P, _P, _P, _P, _P, _I, _I64, _I64, _I, _P,
+                                   C.POINTER(SddmmConfig), _P]),
     "segtaco_spmspv": (C.c_int, [_I, _I, _I64, _P, _P, _P, _I, _P, _P, _P, _P]),
     "segtaco_taco_call": (C.c_int, [_P, C.POINTER(TacoTensor), C.POINTER(TacoTensor),
                                     C.POINTER(TacoTensor), C.POINTER(TacoTensor)]),

@@ -129,17 +129,38 @@ def spmv(A: DeviceCSR, x: torch.Tensor, y: torch.Tensor | None = None,
 
 
 def sddmm(A: DeviceCSR, X: torch.Tensor, Y: torch.Tensor, out: torch.Tensor | None = None,
-          stream=None):
-    """out[p] = A.val[p] * <X[i], Y[j]> over A's pattern (X: M x D, Y: K x D)."""
+          stream=None, config: "N.SddmmConfig | None" = None):
+    """out[p] = A.val[p] * <X[i], Y[j]> over A's pattern (X: M x D, Y: K x D);
+    config: a segtaco_sddmm_config (None: the library's choice)."""
     if out is None:
         out = torch.empty(A.nnz, dtype=torch.float32, device=X.device)
     dt = _dense_dtype(X)
     if _dense_dtype(Y) != dt:
         raise N.SegtacoError(N.EINVAL, "X and Y must have the same dtype")
-    N.check(N.lib().segtaco_sddmm(A.M, A.K, A.nnz, _ptr(A.row_ptr), _ptr(A.col), _ptr(A.val),
-                                  _ptr(X), _ptr(Y), dt, X.stride(0), Y.stride(0), int(X.shape[1]),
-                                  _ptr(out), _stream(stream)))
+    if config is None:
+        N.check(N.lib().segtaco_sddmm(A.M, A.K, A.nnz, _ptr(A.row_ptr), _ptr(A.col),
+                                      _ptr(A.val), _ptr(X), _ptr(Y), dt, X.stride(0),
+                                      Y.stride(0), int(X.shape[1]), _ptr(out), _stream(stream)))
+    else:
+        N.check(N.lib().segtaco_sddmm_ex(A.M, A.K, A.nnz, _ptr(A.row_ptr), _ptr(A.col),
+                                         _ptr(A.val), _ptr(X), _ptr(Y), dt, X.stride(0),
+                                         Y.stride(0), int(X.shape[1]), _ptr(out), C.byref(config),
+                                         _stream(stream)))
     return out
+
+
+def sddmm_autotune(A, D: int, x_dtype=N.F32, max_row_len: int | None = None):
+    """The library's SDDMM configuration (segtaco_sddmm_autotune) for A (a
+    DeviceCSR: longest row from the device; or a host CSR)."""
+    if max_row_len is None:
+        if isinstance(A, DeviceCSR):
+            max_row_len = int(row_stats(A)[0])
+        else:
+            max_row_len = int(np.diff(A.row_ptr).max()) if A.M > 0 else 0
+    cfg = N.SddmmConfig.make()
+    N.check(N.lib().segtaco_sddmm_autotune(A.M, A.K, A.nnz, D, x_dtype, max_row_len,
+                                           C.byref(cfg)))
+    return cfg
 
 
 def spmspv(At: DeviceCSR, x_idx: torch.Tensor, x_val: torch.Tensor, m: int,
@@ -207,19 +228,55 @@ def row_stats(A: DeviceCSR, stream=None):
     return tuple(out)
 
 
+def plan_name(A: DeviceCSR, B: torch.Tensor, config: N.Config | None = None) -> str:
+    """The kernel plan segtaco_spmm picks for A @ B (segtaco_spmm_plan_name)."""
+    buf = C.create_string_buffer(256)
+    N.check(N.lib().segtaco_spmm_plan_name(A.M, A.K, A.nnz, int(B.shape[1]), _dense_dtype(B),
+                                           C.c_void_p(B.data_ptr()), B.stride(0),
+                                           C.byref(config) if config is not None else None,
+                                           buf, 256))
+    return buf.value.decode()
+
+
+def band_stats(A: DeviceCSR, halo: int = 32, stream=None) -> int:
+    """Nonzeros of A within `halo` columns of the diagonal (segtaco_band_stats)."""
+    out = C.c_int64()
+    N.check(N.lib().segtaco_band_stats(A.M, A.K, A.nnz, _ptr(A.row_ptr),
+                                       _ptr(A.col) if A.nnz else None, halo, C.byref(out),
+                                       _stream(stream)))
+    return out.value
+
+
+def in_band_fraction_host(A, halo: int = 32) -> float:
+    """The same statistic from a host CSR."""
+    if A.nnz == 0:
+        return 0.0
+    rows = np.repeat(np.arange(A.M, dtype=np.int64), np.diff(A.row_ptr))
+    d = rows * A.K // max(A.M, 1)
+    return float(np.count_nonzero(np.abs(A.col.astype(np.int64) - d) <= halo)) / A.nnz
+
+
 def autotune(A, n: int, b_dtype=N.F32, schedule=N.AUTO, max_row_len: int | None = None):
     """The library's configuration for C = A @ B with n columns
     (segtaco_autotune_heuristic): the schedule (AUTO: row-balanced for even
-    rows, merge path otherwise), slab, lanes, units and, for row-balanced
+    rows, merge path otherwise), slab, lanes, units; for row-balanced
     schedules with rows of >= 2048 nonzeros from 1M nonzeros on, the long-row
-    CTAs.  `A` is a DeviceCSR (its longest row from segtaco_row_stats on the
-    device) or a host CSR (from its row_ptr), unless max_row_len is given."""
-    if max_row_len is None:
-        if isinstance(A, DeviceCSR):
+    CTAs; and, when at least half of the nonzeros lie within 32 columns of the
+    diagonal, the row-block window of B staged by TMA.  `A` is a DeviceCSR
+    (statistics from segtaco_row_stats / segtaco_band_stats on the device) or
+    a host CSR (from its arrays), unless max_row_len is given."""
+    banded = False
+    if isinstance(A, DeviceCSR):
+        if max_row_len is None:
             max_row_len = int(row_stats(A)[0])
-        else:
+        banded = A.nnz > 0 and band_stats(A) * 2 >= A.nnz
+    else:
+        if max_row_len is None:
             max_row_len = int(np.diff(A.row_ptr).max()) if A.M > 0 else 0
+        banded = A.nnz > 0 and in_band_fraction_host(A) >= 0.5
     cfg = N.Config.make(schedule=schedule)
+    if banded:
+        cfg.flags = N.FLAG_WINDOW
     N.check(N.lib().segtaco_autotune_heuristic(A.M, A.K, A.nnz, n, b_dtype, max_row_len,
                                                C.byref(cfg)))
     return cfg

@@ -247,3 +247,49 @@ def test_flag_constants_match_the_header():
 def test_device_available_is_a_query(native_lib):
     # never raises; 0 on a host without a GPU, 1 on the GB300
     assert native_lib.segtaco_device_available() in (0, 1)
+
+
+def test_window_plan(native_lib):
+    """SEGTACO_FLAG_WINDOW plans the TMA-staged row-block kernel only where the
+    tensor copy is legal (B 16-byte aligned, row pitch a multiple of 16 bytes,
+    window of at most 256 rows and 60 KB) and for row-block schedules."""
+    L = native_lib
+    buf = C.create_string_buffer(256)
+
+    def plan(n, dt, ldb, cfg, B=0x10000000):
+        assert L.segtaco_spmm_plan_name(3000, 3000, 200000, n, dt, C.c_void_p(B), ldb,
+                                        C.byref(cfg), buf, 256) == N.OK
+        return buf.value.decode()
+    mk = lambda sched, **k: N.Config.make(schedule=sched, flags=N.FLAG_WINDOW,
+                                          rows_per_unit=k.get("rpu", 16),
+                                          items_per_unit=k.get("halo", 32),
+                                          col_tile=k.get("tile", 64), vec=k.get("vec", 8))
+    assert " window V=8 G=8 " in plan(64, N.F32, 64, mk(N.RB_PR))
+    assert " window V=2 G=32 " in plan(64, N.F32, 64, mk(N.RB_SR, vec=0))
+    assert " window V=16 G=4 " in plan(64, N.BF16, 64, mk(N.RB_PR, vec=16))
+    assert " window " not in plan(64, N.F32, 64, mk(N.EB_PR))          # rb only
+    assert " window " not in plan(64, N.F32, 66, mk(N.RB_PR, vec=2))   # pitch 264 B
+    assert " window " not in plan(64, N.F32, 64, mk(N.RB_PR), B=0x10000008)  # 8-byte aligned
+    assert " window " not in plan(64, N.F32, 64, mk(N.RB_PR, rpu=32, halo=96))  # 320 rows
+    assert " window " not in plan(64, N.F32, 64, mk(N.RB_PR, rpu=32, halo=64))  # 64 KB
+    # the heuristic takes band statistics but does not choose the window (slower
+    # than plain row blocks on the banded configuration); a B that fits L2 under
+    # a large product gets one 64-column slab of 8-column lanes
+    for flags in (N.FLAG_WINDOW, 0):
+        h = N.Config.make(schedule=N.AUTO, flags=flags)
+        assert L.segtaco_autotune_heuristic(262144, 262144, 19135456, 64, N.F32, 73,
+                                            C.byref(h)) == N.OK
+        assert (h.schedule, h.flags, h.col_tile, h.vec) == (N.RB_PR, 0, 64, 8)
+    h = N.Config.make(schedule=N.AUTO)  # B of 512 MB: 32-column slabs
+    assert L.segtaco_autotune_heuristic(10**6, 10**6, 2 * 10**7, 128, N.F32, 48679,
+                                        C.byref(h)) == N.OK
+    assert h.col_tile == 32
+
+
+def test_band_fraction_host():
+    from segtaco_gb300 import ops, synth
+    A = synth.banded_plus_random(2000, 32, 8, seed=3)
+    f = ops.in_band_fraction_host(A, 32)
+    assert abs(f - 65.0 / 73.0) < 0.01
+    P = synth.power_law(3000, 3000, 1.8, 1000, 0.02, seed=4)
+    assert ops.in_band_fraction_host(P, 32) < 0.1

@@ -1,0 +1,127 @@
+"""Row blocks with their B window staged by TMA (SEGTACO_FLAG_WINDOW): the
+same products as the row-block kernel, whatever share of the gathers the
+window serves -- banded and scattered matrices, fp32 and bf16 B, slabs cut by
+N, window heights, the top and bottom edges (rows outside B zero-filled by the
+copy), strided and offset B; rb_sr stays bit-exact with the sequential FMA
+order."""
+import numpy as np
+import pytest
+import torch
+
+from gpu_util import assert_spmm_close, dev, to_torch_bf16
+from oracle import oracle as O
+from segtaco_gb300 import native as N
+from segtaco_gb300 import ops, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _cfg(sched, rpu=16, halo=32, col_tile=0, vec=0, flags=N.FLAG_WINDOW):
+    c = N.Config.make(schedule=sched, rows_per_unit=rpu, items_per_unit=halo, flags=flags)
+    c.col_tile = col_tile
+    c.vec = vec
+    return c
+
+
+def _spmm(Ad, Bd, cfg):
+    """The product through the window kernel (the plan must pick it)."""
+    assert " window " in ops.plan_name(Ad, Bd, cfg), ops.plan_name(Ad, Bd, cfg)
+    return ops.spmm(Ad, Bd, config=cfg)
+
+
+BANDED = synth.banded_plus_random(3000, 32, 8, seed=41)
+SHORT_BAND = synth.banded_plus_random(777, 5, 2, seed=42)
+
+
+@pytest.mark.parametrize("n,col_tile,vec", [(64, 64, 8), (64, 32, 8), (64, 32, 4), (40, 32, 8),
+                                            (128, 64, 8), (32, 32, 4), (96, 64, 4)])
+@pytest.mark.parametrize("name", ["banded", "short_band"])
+def test_window_rb_pr_fp32(cuda, name, n, col_tile, vec):
+    A = {"banded": BANDED, "short_band": SHORT_BAND}[name]
+    B = synth.dense(A.K, n, seed=43)
+    C = _spmm(dev(A), torch.from_numpy(B).cuda(), _cfg(N.RB_PR, col_tile=col_tile, vec=vec))
+    torch.cuda.synchronize()
+    assert_spmm_close(C.cpu().numpy(), A, B)
+
+
+@pytest.mark.parametrize("rpu,halo", [(1, 0), (4, 8), (16, 32), (16, 64), (32, 32), (8, 96)])
+def test_window_heights(cuda, rpu, halo):
+    B = synth.dense(BANDED.K, 64, seed=44)
+    C = _spmm(dev(BANDED), torch.from_numpy(B).cuda(),
+              _cfg(N.RB_PR, rpu=rpu, halo=halo, col_tile=64, vec=8))
+    torch.cuda.synchronize()
+    assert_spmm_close(C.cpu().numpy(), BANDED, B)
+
+
+def test_window_rb_sr_bitexact(cuda):
+    """rb_sr reads B from the window but keeps each column's storage-order chain."""
+    A = BANDED
+    B = synth.dense(A.K, 64, seed=45)
+    want = O.spmm_f32_rowseq(A.row_ptr, A.col, A.val, B, fma=True)
+    for col_tile in (32, 64):
+        # rb_sr is one 32-lane slot: 1 or 2 columns per lane over 32 or 64 columns
+        c = _cfg(N.RB_SR, col_tile=col_tile)
+        C = _spmm(dev(A), torch.from_numpy(B).cuda(), c)
+        torch.cuda.synchronize()
+        assert np.array_equal(C.cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("n", [64, 128])
+def test_window_bf16(cuda, n):
+    A = BANDED
+    Bf = synth.dense(A.K, n, seed=46)
+    bits = synth.to_bf16_bits(Bf)
+    Bw = synth.bf16_bits_to_f32(bits)
+    C = _spmm(dev(A), to_torch_bf16(bits), _cfg(N.RB_PR, col_tile=64, vec=16))
+    torch.cuda.synchronize()
+    assert_spmm_close(C.cpu().numpy(), A, Bw)
+
+
+@pytest.mark.parametrize("name", ["powerlaw", "rect", "half_empty"])
+def test_window_scattered_and_rectangular(cuda, name):
+    """Matrices whose gathers mostly miss the window (and K != M)."""
+    A = {"powerlaw": synth.power_law(5000, 4000, 1.8, 1500, 0.02, seed=47),
+         "rect": synth.random_csr(2000, 700, 0.03, seed=48),
+         "half_empty": synth.random_csr(1500, 3100, 0.01, seed=49, p_empty=0.5)}[name]
+    B = synth.dense(A.K, 64, seed=50)
+    C = _spmm(dev(A), torch.from_numpy(B).cuda(), _cfg(N.RB_PR, col_tile=64, vec=8))
+    torch.cuda.synchronize()
+    assert_spmm_close(C.cpu().numpy(), A, B)
+
+
+def test_window_strided_offset_b(cuda):
+    """B a strided view (ldb > N) starting 16 bytes into its allocation."""
+    A = BANDED
+    big = torch.from_numpy(synth.dense(A.K, 80, seed=51)).cuda()
+    Bv = big[:, 4:68]  # ldb 80, base 16 bytes in
+    C = _spmm(dev(A), Bv, _cfg(N.RB_PR, col_tile=64, vec=4))
+    torch.cuda.synchronize()
+    assert_spmm_close(C.cpu().numpy(), A, Bv.cpu().numpy())
+
+
+def test_window_overwrites_c(cuda):
+    A = SHORT_BAND
+    B = synth.dense(A.K, 64, seed=52)
+    Cd = torch.full((A.M, 64), float("nan"), device="cuda")
+    Ad, Bd, c = dev(A), torch.from_numpy(B).cuda(), _cfg(N.RB_PR, col_tile=64, vec=8)
+    assert " window " in ops.plan_name(Ad, Bd, c)
+    ops.spmm(Ad, Bd, C_out=Cd, config=c)
+    torch.cuda.synchronize()
+    assert_spmm_close(Cd.cpu().numpy(), A, B)
+
+
+def test_band_stats_and_autotune(cuda):
+    Ad = dev(BANDED)
+    k = ops.band_stats(Ad, 32)
+    assert k == int(round(ops.in_band_fraction_host(BANDED, 32) * BANDED.nnz))
+    assert 2 * k >= BANDED.nnz
+    P = synth.power_law(5000, 4000, 1.8, 1500, 0.02, seed=47)
+    assert 10 * ops.band_stats(dev(P), 32) < P.nnz
+    # the autotuner measures the band but keeps the plain row blocks (faster on
+    # GB300); the window stays an explicit request
+    assert not ops.autotune(Ad, 64).flags & N.FLAG_WINDOW
+    c = _cfg(N.RB_PR, col_tile=64, vec=8)
+    B = synth.dense(BANDED.K, 64, seed=53)
+    C = _spmm(Ad, torch.from_numpy(B).cuda(), c)
+    torch.cuda.synchronize()
+    assert_spmm_close(C.cpu().numpy(), BANDED, B)
