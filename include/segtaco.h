@@ -80,6 +80,11 @@ extern "C" {
                                       segtaco_autotune_heuristic sets it when
                                       the longest row reaches that length      */
 
+#define SEGTACO_FLAG_SLOT_WALK 256u /* eb schedules: every slot of a warp walks its
+                                      own merge-path chunk (items_per_unit items,
+                                      0 = 64) in merge order, each row of a chunk
+                                      one sequential chain; rows cut by chunk
+                                      edges are combined by atomics */
 #define SEGTACO_FLAG_WINDOW 128u /* rb schedules: each CTA of 4 * rows_per_unit rows
                                      stages the B rows [i0 - H, i1 + H) of its column
                                      slab in shared memory with one TMA tensor copy

@@ -88,7 +88,12 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
   if (schedule == SEGTACO_AUTO) schedule = SEGTACO_EB_PR;
   if (schedule < SEGTACO_RB_SR || schedule > SEGTACO_EB_PR)
     return set_error(SEGTACO_EINVAL, "unknown schedule %d", schedule);
-  const bool sequential = schedule == SEGTACO_RB_SR || schedule == SEGTACO_EB_SR;
+  // The slot walk keeps every row of a chunk in one slot, in storage order,
+  // so eb_sr may use several slots there; elsewhere a sequential schedule is
+  // one slot of 32 lanes.
+  const bool slot_walk = (c.flags & SEGTACO_FLAG_SLOT_WALK) &&
+                         (schedule == SEGTACO_EB_SR || schedule == SEGTACO_EB_PR);
+  const bool sequential = (schedule == SEGTACO_RB_SR || schedule == SEGTACO_EB_SR) && !slot_walk;
   // Slab width W = G*V columns.  Sequential schedules use one slot (G = 32);
   // parallel ones use P = 32/G >= 2 slots, by default a 128-byte B segment per
   // nonzero (32 fp32 / 64 bf16 columns).
@@ -142,6 +147,16 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
                              (schedule == SEGTACO_EB_SR && G == 32 &&
                               !(c.flags & SEGTACO_FLAG_ROW_WALK)));
   plan->walk = flat ? 2 : (plan->deep && wide ? 1 : 0);
+  // The slot walk (every slot its own merge-path chunk) on request, for the
+  // element-balanced schedules and the lane shapes it is compiled for.
+  const bool eb = schedule == SEGTACO_EB_SR || schedule == SEGTACO_EB_PR;
+  if ((c.flags & SEGTACO_FLAG_SLOT_WALK) && eb && !plan->use_tma) {
+    const int k = V * 100 + G;
+    const bool ok = esz == 4 ? (k == 804 || k == 408 || k == 808 || k == 404 || k == 416 ||
+                                k == 101)
+                             : (k == 1604 || k == 804 || k == 808);
+    if (ok) plan->walk = 3;
+  }
   plan->rows_per_unit = c.rows_per_unit > 0 ? c.rows_per_unit : 1;
   plan->items_per_unit = 0;
   plan->nchunks = (M + plan->rows_per_unit - 1) / plan->rows_per_unit;  // rb: row blocks
@@ -149,7 +164,9 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
   plan->long_row = 0;
   plan->px_entries = plan->py_entries = 0;
   if (schedule == SEGTACO_EB_SR || schedule == SEGTACO_EB_PR) {
-    long long D = c.items_per_unit > 0 ? c.items_per_unit : 512;
+    // merge-path items per chunk: one chunk per warp (512), or per slot in the
+    // slot walk (64, so a warp still covers about 512)
+    long long D = c.items_per_unit > 0 ? c.items_per_unit : (plan->walk == 3 ? 64 : 512);
     if (D < 1) D = 1;
     const long long total = (long long)M + nnz;
     long long nch = (total + D - 1) / D;

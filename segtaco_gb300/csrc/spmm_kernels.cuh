@@ -612,9 +612,126 @@ __device__ __forceinline__ void spmm_flat_unit(const SpmmArgs<BT> &a, long long 
     atomic_add_c<V>(a.C + (long long)x1 * a.ldc + col0, acc);
 }
 
-// Walks of a unit: the row walk with 4 or 8 loads in flight per lane, or the
-// flat walk (chosen by the planner, api.cu).
-constexpr int kWalkRows = 0, kWalkRowsDeep = 1, kWalkFlat = 2;
+// Slot walk of merge-path chunks: slot s of warp w owns chunk w*P + s (its
+// own row range and nonzero range) and walks it in merge order on its own --
+// each step takes the slot's next nonzero, and a position at or past the end
+// of the slot's current row first stores that row (and any empty rows after
+// it).  A round trip issues U positions per slot (U * P per warp) whatever
+// the row lengths, so short rows cost no more than long ones, and no fold is
+// needed: each row of a chunk is one sequential fmaf chain in storage order
+// (so it also serves the sequential schedule, eb_sr, on narrow slabs).  A row
+// cut by a chunk edge is zeroed by the partition kernel and receives
+// red.global.add from every chunk holding part of it.
+//
+// Per slot, row ends come from a window of G of them (lane g holds the end of
+// row wr + g) and the next G, read one window ahead; the slot's U column
+// indices and values of a round trip are one coalesced load by its lanes and
+// reach the other lanes of the slot by shuffles of width G.
+template <typename BT, int V, int G>
+__device__ __forceinline__ void spmm_slot_unit(const SpmmArgs<BT> &a, long long w, int slab,
+                                               int lane) {
+  constexpr int P = 32 / G;  // slots (one chunk each)
+  // Positions per slot per round trip: one per lane of the slot, at most 8
+  // and at most 128 bytes of B in flight per lane.
+  constexpr int UB_ = 128 / (V * (int)sizeof(BT)) < 1 ? 1 : 128 / (V * (int)sizeof(BT));
+  constexpr int U = G < 8 ? (G < UB_ ? G : UB_) : (8 < UB_ ? 8 : UB_);
+  using D = Dense<BT, V>;
+  const unsigned FULL = 0xffffffffu;
+  const int slot = lane / G, gl = lane & (G - 1);
+  const unsigned smask = group_mask<G>(lane);
+  const int M = a.M;
+  const int col0 = slab * (G * V) + gl * V;
+  const bool active = col0 < a.N;
+  const uint64_t pol = l2_policy(a.l2_hints);
+  const BT *Bc = a.B + (active ? col0 : 0);  // lanes past N load column 0, never store
+  const unsigned ldb = (unsigned)a.ldb;
+
+  const long long c = w * P + slot;
+  const bool has = c < a.units;
+  int x = 0, x1 = 0, y = 0, y1 = 0;
+  if (has) {
+    x = __ldg(a.part_x + c);
+    y = __ldg(a.part_y + c);
+    x1 = __ldg(a.part_x + c + 1);
+    y1 = __ldg(a.part_y + c + 1);
+  }
+  // Row x began in an earlier chunk; row x1 holds nonzeros here and ends later.
+  const bool head_split = has && x < M && __ldg(a.row_ptr + x) < y;
+  const bool tail_open = has && x1 < M && __ldg(a.row_ptr + x1) < y1;
+  auto rp = [&](long long i) -> int { return i <= M ? __ldg(a.row_ptr + i) : INT_MAX; };
+  int wr = x;                            // lane gl: end of row wr + gl
+  int rw_cur = has ? rp((long long)wr + 1 + gl) : INT_MAX;
+  int rw_nxt = has ? rp((long long)wr + 1 + G + gl) : INT_MAX;
+  // End of row r (r >= wr; the slot's lanes move together).
+  auto row_end = [&](int r) -> int {
+    while (r - wr >= G) {
+      wr += G;
+      rw_cur = rw_nxt;
+      rw_nxt = rp((long long)wr + 1 + G + gl);
+    }
+    return __shfl_sync(smask, rw_cur, r - wr, G);
+  };
+  float acc[V];
+  zero<V>(acc);
+  auto flush = [&](int r) {
+    if (active) {
+      float *dst = a.C + (long long)r * a.ldc + col0;
+      if ((r == x && head_split) || (r == x1 && tail_open))
+        atomic_add_c<V>(dst, acc);
+      else
+        store_c<V>(dst, acc);
+    }
+    zero<V>(acc);
+  };
+  int row = x;
+  int rend = has ? row_end(row) : INT_MAX;
+  int p = y;
+  for (;;) {
+    const bool more = has && p < y1;
+    if (!__any_sync(FULL, more)) break;
+    // The slot's next U column indices and values (lane gl < U: position p + gl).
+    const int q = p + gl;
+    const bool okq = more && gl < U && q < y1;
+    const int mc = okq ? ld_stream(a.col + q) : 0;
+    const float mv = okq ? ld_val(a.val, q) : 0.0f;
+    typename D::raw_t b[U];
+    float vv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int j = __shfl_sync(FULL, mc, u, G);
+      vv[u] = __shfl_sync(FULL, mv, u, G);
+      b[u] = D::load(Bc + (size_t)(unsigned)j * ldb, pol);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int pos = p + u;
+      if (more && pos < y1) {
+        while (pos >= rend) {  // rows ending before this position (empty ones too)
+          flush(row);
+          ++row;
+          rend = row_end(row);
+        }
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc[v] = fmaf(vv[u], D::get(b[u], v), acc[v]);
+      }
+    }
+    p += U;
+  }
+  if (has) {
+    // Rows that end inside the chunk after its last nonzero (empty or not),
+    // then the row still open at the chunk's end.
+    while (row < x1) {
+      flush(row);
+      ++row;
+    }
+    if (tail_open) flush(x1);
+  }
+}
+
+// Walks of a unit: the row walk with 4 or 8 loads in flight per lane, the
+// flat walk, or the slot walk over merge-path chunks (chosen by the planner,
+// api.cu).
+constexpr int kWalkRows = 0, kWalkRowsDeep = 1, kWalkFlat = 2, kWalkSlots = 3;
 
 // CTAs of the SpMM kernels: 4 warps each, so a CTA that finishes early frees
 // its slot soon (warps of a CTA walk units of uneven cost).  32 warps per SM
@@ -634,6 +751,11 @@ __global__ void __launch_bounds__(kSpmmCta, spmm_min_ctas<V, G, WALK == kWalkRow
                                                                   (WALK == kWalkFlat && V == 8)>())
     spmm_seg_kernel(SpmmArgs<BT> a) {
   const long long w = (long long)blockIdx.x * kSpmmWarps + threadIdx.x / 32;
+  if constexpr (WALK == kWalkSlots) {  // a.units chunks, 32 / G per warp
+    if (w * (32 / G) >= a.units) return;
+    spmm_slot_unit<BT, V, G>(a, w, blockIdx.y, threadIdx.x & 31);
+    return;
+  }
   if (w >= a.units) return;  // whole warp leaves together
   if (WALK == kWalkFlat)
     spmm_flat_unit<BT, V, G, ROWS>(a, w, blockIdx.y, threadIdx.x & 31);

@@ -54,11 +54,14 @@ inline void launch_seg(void (*kern)(SpmmArgs<BT>), dim3 grid, cudaStream_t s,
   cudaLaunchKernelEx(&cfg, kern, a);  // errors surface in the caller's check_launch
 }
 
-// One warp per unit (x), one column slab per blockIdx.y.
+// One warp per unit (x), one column slab per blockIdx.y; the slot walk packs
+// 32 / G units (one per slot) into a warp.
 inline dim3 spmm_grid(const SpmmLaunch &L) {
   const long long W = (long long)L.V * L.G;
   const unsigned slabs = (unsigned)((L.N + W - 1) / W);
-  long long x = (L.units + kSpmmWarps - 1) / kSpmmWarps;
+  const long long per_warp = L.walk == kWalkSlots ? 32 / L.G : 1;
+  const long long warps = (L.units + per_warp - 1) / per_warp;
+  long long x = (warps + kSpmmWarps - 1) / kSpmmWarps;
   if (x < 1) x = 1;
   return dim3((unsigned)x, slabs, 1);
 }
@@ -84,12 +87,43 @@ inline dim3 spmm_grid(const SpmmLaunch &L) {
   SEGTACO_WALK_CASE(BT, 4, R, WALK) SEGTACO_WALK_CASE(BT, 8, R, WALK)                   \
   SEGTACO_WALK_CASE(BT, 16, R, WALK) SEGTACO_WALK_CASE(BT, 32, R, WALK)
 
+// Slot-walk variants (merge-path chunks only).
+#define SEGTACO_SLOT_CASE(BT, V, G)                                                      \
+  case V * 100 + G:                                                                      \
+    launch_seg(spmm_seg_kernel<BT, V, G, false, kWalkSlots>, grid, s, a, L.carveout);    \
+    break;
+#define SEGTACO_SLOT_CASES_F32(BT)                                                       \
+  SEGTACO_SLOT_CASE(BT, 8, 4) SEGTACO_SLOT_CASE(BT, 4, 8) SEGTACO_SLOT_CASE(BT, 8, 8)    \
+  SEGTACO_SLOT_CASE(BT, 4, 4) SEGTACO_SLOT_CASE(BT, 4, 16) SEGTACO_SLOT_CASE(BT, 1, 1)
+#define SEGTACO_SLOT_CASES_BF16(BT)                                                      \
+  SEGTACO_SLOT_CASE(BT, 16, 4) SEGTACO_SLOT_CASE(BT, 8, 4) SEGTACO_SLOT_CASE(BT, 8, 8)
+#define SEGTACO_SLOT_CASES(BT)                                                           \
+  if constexpr (sizeof(BT) == 4) {                                                       \
+    switch (L.V * 100 + L.G) {                                                           \
+      SEGTACO_SLOT_CASES_F32(BT)                                                         \
+      default:                                                                           \
+        return set_error(SEGTACO_EUNSUPPORTED, "slot walk: no variant V=%d G=%d", L.V, L.G); \
+    }                                                                                    \
+  } else {                                                                               \
+    switch (L.V * 100 + L.G) {                                                           \
+      SEGTACO_SLOT_CASES_BF16(BT)                                                        \
+      default:                                                                           \
+        return set_error(SEGTACO_EUNSUPPORTED, "slot walk: no variant V=%d G=%d", L.V, L.G); \
+    }                                                                                    \
+  }
+
 // Defines int NAME(const SpmmLaunch&, cudaStream_t) for one (dtype, unit kind).
 #define SEGTACO_DEFINE_SPMM_LAUNCHER(NAME, BT, VG_LIST, ROWS)                             \
   namespace segtaco {                                                                     \
   int NAME(const SpmmLaunch &L, cudaStream_t s) {                                         \
     const SpmmArgs<BT> a = make_spmm_args<BT>(L);                                         \
     const dim3 grid = spmm_grid(L);                                                       \
+    if constexpr (!ROWS) {                                                                \
+      if (L.walk == kWalkSlots) {                                                         \
+        SEGTACO_SLOT_CASES(BT)                                                            \
+        return check_launch(#NAME);                                                       \
+      }                                                                                   \
+    }                                                                                     \
     if (L.walk != kWalkRows && L.V * (int)sizeof(BT) == 16) {                            \
       if (L.walk == kWalkRowsDeep) {                                                      \
         switch (L.G) {                                                                    \

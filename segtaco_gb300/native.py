@@ -39,6 +39,7 @@ FLAG_ROW_WALK = 16
 FLAG_FLAT_WALK = 32
 FLAG_LONG_ROWS = 64
 FLAG_WINDOW = 128
+FLAG_SLOT_WALK = 256
 
 
 class SegtacoError(RuntimeError):
