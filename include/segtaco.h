@@ -69,14 +69,17 @@ extern "C" {
                                       across rows (the default for eb_sr with
                                       16-byte vectors)                           */
 #define SEGTACO_FLAG_LONG_ROWS 64u /* rb schedules with nnz >= 1M: rows of at
-                                      least items_per_unit nonzeros go to
-                                      long-row CTAs (see items_per_unit) on a
-                                      side stream the library forks from the
+                                      least items_per_unit nonzeros are taken
+                                      out of the row blocks (see
+                                      items_per_unit).  rb_sr: long-row CTAs on
+                                      a side stream the library forks from the
                                       call's stream and joins before returning
                                       (created by the first such call on a
                                       host thread and device; a call captured
                                       into a graph before that runs both
-                                      kernels on the call's stream);
+                                      kernels on the call's stream).  rb_pr:
+                                      pieces of 512 nonzeros inside the
+                                      row-block launch, no side stream;
                                       segtaco_autotune_heuristic sets it when
                                       the longest row reaches that length      */
 
@@ -104,14 +107,20 @@ typedef struct segtaco_config {
                              32-byte aligned).  The planner narrows it to what
                              N, ldb and the pointers allow                     */
   int32_t rows_per_unit;  /* rb: rows handled by one lane group / warp            */
-  int32_t items_per_unit; /* eb: merge-path items (rows + nonzeros) per unit.
+  int32_t items_per_unit; /* eb: merge-path items (rows + nonzeros) per unit
+                             (0: 512, fewer for small products).
                              rb with SEGTACO_FLAG_LONG_ROWS and nnz >= 1M:
-                             rows of at least this many nonzeros (0 = 2048) go
-                             to long-row CTAs that stage B rows in shared
-                             memory for the whole CTA (rb_sr: each column
-                             still summed in storage order; rb_pr: four warps'
-                             partial sums folded); the row-block kernel runs
-                             beside them on the other rows                   */
+                             rows of at least this many nonzeros (0 = 2048
+                             for rb_sr, 512 for rb_pr).
+                             rb_sr: to long-row CTAs that stage B rows in
+                             shared memory for the whole CTA, each column
+                             still summed in storage order, beside the
+                             row-block kernel.  rb_pr: split into pieces of
+                             512 nonzeros that warps of the row-block launch
+                             take over the same column slabs; each piece's
+                             partial row goes to the workspace and the last
+                             piece of a row sums them in piece order, so the
+                             result does not vary from run to run          */
   uint32_t flags;         /* SEGTACO_FLAG_*                                        */
   int32_t depth;          /* row walk: dense loads in flight per lane (0 = 4, 4, 8) */
 } segtaco_config;
@@ -157,8 +166,10 @@ int segtaco_spmm(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr, cons
  * start-up, a caller that cannot take an allocation's device-wide sync -- the
  * element-balanced schedules' scratch (merge-path chunk coordinates) and
  * the row-block schedules' list of long rows come from a fixed 2 MiB array in
- * the library's device memory instead of a workspace (a list of more than
- * 262,143 entries is not made: every row then stays in the row-block kernel).
+ * the library's device memory instead of a workspace (rb_pr's pieces, whose
+ * partial rows do not fit there, give way to the long-row CTAs; a list of more
+ * than 262,143 entries is not made: every row then stays in the row-block
+ * kernel).
  * Limit: at most 262,143 merge-path chunks, i.e. ceil((M + nnz) /
  * items_per_unit) <= 262,143 (M + nnz <= ~134M at the default 512 items);
  * larger problems get SEGTACO_EINVAL.  The first call on each
@@ -180,7 +191,8 @@ int segtaco_spmm_noalloc(int32_t M, int32_t K, int64_t nnz, const int32_t *row_p
  * segtaco_spmm with SEGTACO_FLAG_PARTITION_READY, the same config, workspace,
  * A, C and N runs only the product kernel.  Must be repeated before every
  * product (the zeroing belongs to one product).  For rb schedules with
- * long-row CTAs (see items_per_unit) it lists the long rows instead; no-op
+ * long rows (see items_per_unit) it lists the long rows (rb_sr) or their
+ * pieces (rb_pr) instead, and that list may serve repeated products; no-op
  * for the other rb cases.  workspace must be the caller's (not NULL). */
 int segtaco_spmm_partition(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr,
                            float *C, int64_t ldc, int32_t N, int32_t b_dtype,

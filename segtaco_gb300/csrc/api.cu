@@ -64,7 +64,8 @@ static bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
 
 
 int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, long long ldc,
-              const void *B, const float *C, const segtaco_config *cfg, SpmmPlan *plan) {
+              const void *B, const float *C, const segtaco_config *cfg, SpmmPlan *plan,
+              bool pieces) {
   segtaco_config c{};
   c.schedule = SEGTACO_AUTO;
   if (cfg) c = *cfg;
@@ -162,11 +163,15 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
   plan->nchunks = (M + plan->rows_per_unit - 1) / plan->rows_per_unit;  // rb: row blocks
   plan->workspace = 0;
   plan->long_row = 0;
+  plan->piece_len = 0;
   plan->px_entries = plan->py_entries = 0;
   if (schedule == SEGTACO_EB_SR || schedule == SEGTACO_EB_PR) {
-    // merge-path items per chunk: one chunk per warp (512), or per slot in the
-    // slot walk (64, so a warp still covers about 512)
-    long long D = c.items_per_unit > 0 ? c.items_per_unit : (plan->walk == 3 ? 64 : 512);
+    // merge-path items per chunk: one chunk per warp (512, fewer for small
+    // products), or per slot in the slot walk (64, so a warp still covers
+    // about 512)
+    long long D = c.items_per_unit > 0   ? c.items_per_unit
+                  : plan->walk == 3 ? 64
+                                    : default_chunk_items(M, nnz);
     if (D < 1) D = 1;
     const long long total = (long long)M + nnz;
     long long nch = (total + D - 1) / D;
@@ -176,10 +181,20 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
     plan->px_entries = plan->py_entries = nch + 1;
   } else if (nnz >= kLongRowsMinNnz && (c.flags & SEGTACO_FLAG_LONG_ROWS) &&
              plan->walk != 2 && !plan->use_tma) {
-    // Long rows to CTAs of their own (spmm_long.cu): their ring copies 16-byte
-    // chunks of B rows, so B, ldb and N must allow 16-byte pieces.
     const int epc = 16 / esz;
-    if (N % epc == 0 && ldb % epc == 0 && ((uintptr_t)B % 16) == 0) {
+    if (schedule == SEGTACO_RB_PR && pieces) {
+      // rb_pr: long rows as pieces of kPieceLen nonzeros in the row-block
+      // launch (spmm_long.cu), over the same column slabs; rows from kPieceLen
+      // nonzeros by default.
+      long long T = c.items_per_unit > 0 ? c.items_per_unit : kPieceLen;
+      if (T > nnz) T = nnz;
+      plan->long_row = (int)T;
+      plan->piece_len = (int)kPieceLen;
+      plan->px_entries = piece_layout(nnz, T, kPieceLen, plan->slabs, W).entries;
+      plan->py_entries = 4;  // the count
+    } else if (N % epc == 0 && ldb % epc == 0 && ((uintptr_t)B % 16) == 0) {
+      // Long rows to CTAs of their own (spmm_long.cu): their ring copies
+      // 16-byte chunks of B rows, so B, ldb and N must allow 16-byte pieces.
       long long T = long_row_threshold(c);
       if (T > nnz) T = nnz;
       long long hi, lo;
@@ -244,6 +259,23 @@ int run_spmm_planned(const SpmmPlan &plan, int M, int K, long long nnz, const in
     case SEGTACO_RB_PR:
       if (L.use_tma) return bf16 ? launch_spmm_tma_bf16(L, true, s) : launch_spmm_tma_f32(L, true, s);
       if (plan.window_halo >= 0) return launch_spmm_window(L, s);
+      if (plan.long_row > 0 && plan.piece_len > 0) {
+        L.long_row = plan.long_row;
+        if (!partition_ready)
+          SEGTACO_TRY(launch_long_pieces_list(row_ptr, M, nnz, plan.long_row, plan.piece_len,
+                                              plan.slabs, plan.W, px, py, s));
+        const PieceLayout pl =
+            piece_layout(nnz, plan.long_row, plan.piece_len, plan.slabs, plan.W);
+        L.piece_len = plan.piece_len;
+        L.pieces = px;
+        L.piece_count = py;
+        L.piece_ctr = reinterpret_cast<unsigned *>(px + pl.ctr);
+        L.piece_part = reinterpret_cast<float *>(px + pl.part);
+        L.piece_cap = pl.cap;
+        L.piece_multi = pl.multi;
+        L.piece_ld = pl.ld;
+        return bf16 ? launch_spmm_bf16_rows(L, s) : launch_spmm_f32_rows(L, s);
+      }
       if (plan.long_row > 0) {
         L.long_row = plan.long_row;
         if (!partition_ready)
@@ -331,8 +363,9 @@ int segtaco_autotune_heuristic(int32_t M, int32_t K, int64_t nnz, int32_t N, int
   // 0.435 ms).  rb_sr's row-block kernel then takes 128-column slabs also for
   // bf16 (8-byte lanes).  Measured on GB300, 1M x 1M power law, N = 128:
   // fp32 2.32 ms (64-column slabs: 2.45), bf16 2.29 ms (256: 2.52).
-  const bool long_rows = (schedule == SEGTACO_RB_SR || schedule == SEGTACO_RB_PR) &&
-                         nnz >= kLongRowsMinNnz && max_row_len >= kLongRowDefault;
+  const bool long_rows =
+      (schedule == SEGTACO_RB_SR || schedule == SEGTACO_RB_PR) && nnz >= kLongRowsMinNnz &&
+      max_row_len >= (schedule == SEGTACO_RB_PR ? kPieceLen : kLongRowDefault);
   if (schedule == SEGTACO_RB_SR && long_rows) cfg->col_tile = 128;
   // fp32 with B beyond L2 (32-column slabs): 8 columns per lane (one 32-byte
   // load, 4 lanes per 128-byte segment, 8 slots), so a warp step covers 8 rows
@@ -358,11 +391,33 @@ int segtaco_autotune_heuristic(int32_t M, int32_t K, int64_t nnz, int32_t N, int
   if (!sequential && esz == 2 && bbytes > 48e6 && N % 16 == 0 && (skewed || nnz >= 4000000))
     cfg->vec = 16;
   // eb: merge-path items per chunk; rb: the long-row threshold.
-  cfg->items_per_unit =
-      (schedule == SEGTACO_RB_SR || schedule == SEGTACO_RB_PR) ? (int)kLongRowDefault : 512;
+  cfg->items_per_unit = (schedule == SEGTACO_RB_SR || schedule == SEGTACO_RB_PR)
+                            ? (int)kLongRowDefault
+                            : (int)default_chunk_items(M, nnz);
   cfg->rows_per_unit = schedule == SEGTACO_RB_PR || schedule == SEGTACO_RB_SR ? 4 : 1;
+  // rb_sr walks its rows one after another in one slot: fewer rows per warp
+  // while the rows are few.  Measured on GB300, 16,384 x 16,384 with 16
+  // nonzeros per row, N = 32: 0.0174 ms with 4 rows, 0.0154 with 2.
+  if (schedule == SEGTACO_RB_SR)
+    while (cfg->rows_per_unit > 1 && M / cfg->rows_per_unit < 8192) cfg->rows_per_unit >>= 1;
   cfg->depth = (schedule == SEGTACO_RB_SR || schedule == SEGTACO_RB_PR) ? 8 : 4;
   cfg->flags = long_rows ? SEGTACO_FLAG_LONG_ROWS : 0;
+  // rb_pr's long rows as pieces of the row-block launch (rows of >= 512
+  // nonzeros); the rows left are short, so a warp takes 32 of them to fill its
+  // slots.  Measured on GB300, 1M x 1M power law, N = 128: 1.69 ms with the
+  // long-row CTAs (threshold 2048, 4 rows per warp), 1.58 with pieces, 1.22
+  // with 32 rows per warp (1.20 with 64; 2 rows: 2.01).  Rows of ~73
+  // nonzeros (banded, N = 64) keep 4: 0.251 ms against 0.266 with 16.
+  if (schedule == SEGTACO_RB_PR && long_rows) {
+    cfg->items_per_unit = (int)kPieceLen;
+    if (mean < 32.0) cfg->rows_per_unit = 32;
+  }
+  // fp32 B beyond L2 under skewed rows: the gathered B rows evict_last in L2
+  // (A and C stream with evict-first loads and stores).  Measured on GB300,
+  // 1M x 1M power law, N = 128, three alternations: eb_pr 1.128 -> 1.110 ms,
+  // rb_pr (pieces, 32 rows per warp) 1.219 -> 1.201; rb_sr unchanged (1.683
+  // / 1.687).
+  if (!sequential && esz == 4 && bbytes > 48e6 && skewed) cfg->flags |= SEGTACO_FLAG_L2_HINTS;
   // Rows known to lie near the diagonal (the caller's segtaco_band_stats):
   // the staged B window is NOT chosen.  Measured on GB300, banded 262,144
   // rows, N = 64: the row-block kernel's gathers of the band already hit L1,
@@ -383,7 +438,7 @@ int segtaco_spmm_plan_name(int32_t M, int32_t K, int64_t nnz, int32_t N, int32_t
   static const char *sched[] = {"rb_sr", "rb_pr", "eb_sr", "eb_pr"};
   const char *kernel = plan.use_tma         ? "tma_ring"
                        : plan.window_halo >= 0 ? "window"
-                       : plan.long_row > 0 ? "long_rows"
+                       : plan.long_row > 0 ? (plan.piece_len > 0 ? "pieces" : "long_rows")
                        : (plan.schedule >= SEGTACO_EB_SR) ? "chunks" : "rows";
   snprintf(out, len, "%s %s V=%d G=%d W=%d slabs=%d walk=%d halo=%d rows_per_unit=%lld",
            sched[plan.schedule], kernel, plan.V, plan.G, plan.W, plan.slabs, plan.walk,
@@ -445,6 +500,9 @@ int segtaco_spmm_partition(int32_t M, int32_t K, int64_t nnz, const int32_t *row
   SEGTACO_TRY(scratch.reserve(plan.workspace));
   int *px = static_cast<int *>(scratch.take(plan.px_entries * sizeof(int)));
   int *py = static_cast<int *>(scratch.take(plan.py_entries * sizeof(int)));
+  if (plan.long_row > 0 && plan.piece_len > 0)
+    return launch_long_pieces_list(row_ptr, M, nnz, plan.long_row, plan.piece_len, plan.slabs,
+                                   plan.W, px, py, s);
   if (plan.long_row > 0) return launch_long_rows_list(row_ptr, M, nnz, plan.long_row, px, py, s);
   return launch_merge_path(row_ptr, M, nnz, plan.items_per_unit, plan.nchunks, px, py, C, ldc, N,
                            s);

@@ -344,7 +344,13 @@ int plan_batch_problem(const segtaco_spmm_problem &p, const segtaco_config *cfg,
   } else {
     c.schedule = SEGTACO_AUTO;
     segtaco_autotune_heuristic(p.M, p.K, p.nnz, p.N, p.b_dtype, max_row_len, &c);
+    // The batch fills the GPU with many problems: no problem needs the small
+    // chunks and row blocks that make one small product fill it alone.
+    if (c.schedule == SEGTACO_RB_SR || c.schedule == SEGTACO_RB_PR) c.rows_per_unit = 4;
   }
+  if ((c.schedule == SEGTACO_EB_SR || c.schedule == SEGTACO_EB_PR) &&
+      (!cfg || c.items_per_unit <= 0))
+    c.items_per_unit = 512;
   c.depth = 0;
   c.flags &= ~(SEGTACO_FLAG_SMEM_RING | SEGTACO_FLAG_TMA_BULK | SEGTACO_FLAG_PARTITION_READY);
   // The persistent kernel walks every row of its items (no long-row CTAs).

@@ -81,6 +81,16 @@ struct SpmmLaunch {
                                // stream or events are created)
   int window_halo = -1;        // >= 0: rb rows with B rows [i0 - halo, i1 + halo) of each
                                // row block staged by TMA (spmm_window.cu)
+  // rb_pr long rows as pieces of piece_len nonzeros in the row-block launch
+  // (spmm_long.cu): (row, first nonzero) pairs, their count, the list capacity.
+  int piece_len = 0;
+  const int *pieces = nullptr;
+  const int *piece_count = nullptr;
+  unsigned *piece_ctr = nullptr;  // per (first piece of a row, slab) counters
+  float *piece_part = nullptr;    // partial rows, piece_ld floats per piece
+  long long piece_cap = 0;        // list entries (both parts)
+  long long piece_multi = 0;      // entries of the front part (rows of several pieces)
+  long long piece_ld = 0;
 };
 // One launcher per (dense type, unit kind); each switches over (V, G).
 int launch_spmm_f32_rows(const SpmmLaunch &L, cudaStream_t s);
@@ -112,13 +122,16 @@ struct SpmmPlan {
   int long_row;              // rb: long-row threshold (0: every row in the row-block kernel)
   bool no_fork = false;      // rb long rows: no side stream (segtaco_spmm_noalloc)
   int window_halo = -1;      // rb: >= 0 stages each row block's B window (spmm_window.cu)
+  int piece_len = 0;         // rb_pr: long rows split into pieces of this many nonzeros
   long long px_entries;      // int32 entries of the first workspace array (eb: chunk-edge
                              // rows; rb long rows: the list of long rows)
   long long py_entries;      // ... of the second (eb: chunk-edge nonzeros; long rows: counters)
   size_t workspace;          // bytes
 };
+// `pieces` false: rb_pr long rows go to the long-row CTAs, as for rb_sr.
 int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, long long ldc,
-              const void *B, const float *C, const segtaco_config *cfg, SpmmPlan *plan);
+              const void *B, const float *C, const segtaco_config *cfg, SpmmPlan *plan,
+              bool pieces = true);
 // Runs a planned SpMM with partition arrays already in `px/py` (eb) or none.
 int run_spmm_planned(const SpmmPlan &plan, int M, int K, long long nnz, const int *row_ptr,
                      const int *col, const float *vals, const void *B, int b_dtype, long long ldb,
@@ -162,12 +175,44 @@ int launch_sddmm(int M, long long nnz, const int *row_ptr, const int *col, const
 // Row-block products below this many nonzeros walk every row in the row-block
 // kernel: the list pass and the fork would cost more than a long row there.
 constexpr long long kLongRowsMinNnz = 1000000;
+// Merge-path items per chunk of a product launched alone: 512 (a warp's
+// chunk), halved down to 32 while the grid would hold fewer than 4,096
+// chunks, so that small products still fill the 152 SMs.  Measured on GB300,
+// 16,384 x 16,384 with 16 nonzeros per row, N = 32 (partition + product):
+// eb_sr 0.0462 -> 0.0240 ms and eb_pr 0.0295 -> 0.0203 ms with 64 items.
+inline long long default_chunk_items(long long M, long long nnz) {
+  long long D = 512;
+  while (D > 32 && (M + nnz) / D < 4096) D >>= 1;
+  return D;
+}
 // Default long-row threshold (items_per_unit = 0).  Measured on GB300 (1M x 1M
 // power law, N = 128, Zipf 1.8 / 1.922, rb_sr): 1024: 2.33 / 1.45 ms, 2048:
 // 2.27 / 1.44, 4096: 2.23 / 1.46.
 constexpr long long kLongRowDefault = 2048;
 inline long long long_row_threshold(const segtaco_config &c) {
   return c.items_per_unit > 0 ? c.items_per_unit : kLongRowDefault;
+}
+// rb_pr splits every row of >= T nonzeros into pieces of S nonzeros.  Rows
+// of more than S nonzeros (n = ceil(len / S) <= 2 len / S pieces each, at most
+// 2 nnz / S in all) take the front of the piece list, each piece with a
+// partial row and a counter per column slab; rows of T .. S nonzeros (at most
+// nnz / T) are one piece each at the back and store directly.  The workspace,
+// in int32 entries from the start of the first array: the (row, first
+// nonzero) pairs, the counters, the partial rows (`ld` floats each, 256-byte
+// aligned).
+constexpr long long kPieceLen = 512;
+struct PieceLayout {
+  long long multi, cap, ld, ctr, part, entries;
+};
+inline PieceLayout piece_layout(long long nnz, long long T, long long S, int slabs, int W) {
+  PieceLayout p;
+  p.multi = 2 * nnz / S + 1;
+  p.cap = p.multi + nnz / T + 1;
+  p.ld = (long long)slabs * W;
+  p.ctr = 2 * p.cap;
+  p.part = (p.ctr + p.multi * slabs + 63) / 64 * 64;
+  p.entries = p.part + p.multi * p.ld;
+  return p;
 }
 // The two parts of the long-row list for threshold T: rows of >= 8T nonzeros
 // (at most nnz / 8T of them) and rows of T .. 8T-1 (at most nnz / T).
@@ -182,6 +227,12 @@ int launch_long_rows_list(const int *row_ptr, int M, long long nnz, int long_row
 // The long-row CTAs for the listed rows, on a side stream forked from `s`, and
 // the row-block kernel `L` (L.long_row set: it skips those rows) on `s`.
 int launch_spmm_long_rows(const SpmmLaunch &L, const int *list, int *counters, cudaStream_t s);
+// rb_pr: lists every row of >= long_row nonzeros as pieces of piece_len
+// nonzeros into `pieces` (piece_layout: the pairs, the counters of each row's
+// first piece cleared here), counting the front and back parts in count[0]
+// and count[1] (cleared here).
+int launch_long_pieces_list(const int *row_ptr, int M, long long nnz, int long_row, int piece_len,
+                            int slabs, int W, int *pieces, int *count, cudaStream_t s);
 
 int launch_spmspv(int M, int K, const int *col_ptr, const int *row_idx, const float *val, int nx,
                   const int *x_idx, const float *x_vals, float *y, cudaStream_t s);

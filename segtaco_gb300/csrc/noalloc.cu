@@ -81,10 +81,14 @@ extern "C" int segtaco_spmm_noalloc(int32_t M, int32_t K, int64_t nnz, const int
                      "segtaco_spmm_noalloc: PARTITION_READY is not supported (shared scratch)");
   SpmmPlan plan;
   SEGTACO_TRY(plan_spmm(M, K, nnz, N, b_dtype, ldb, ldc, B, C, cfg, &plan));
+  if (plan.piece_len > 0 && plan.px_entries > kNoallocEntries)
+    // rb_pr pieces whose partial rows would not fit: the long-row CTAs
+    SEGTACO_TRY(plan_spmm(M, K, nnz, N, b_dtype, ldb, ldc, B, C, cfg, &plan, false));
   plan.no_fork = true;  // rb long rows: no side stream or events, both kernels on `stream`
   if (plan.long_row > 0 && plan.px_entries > kNoallocEntries) {
     // the long-row list would not fit: every row in the row-block kernel
     plan.long_row = 0;
+    plan.piece_len = 0;
     plan.px_entries = plan.py_entries = 0;
     plan.workspace = 0;
   }

@@ -62,7 +62,21 @@ template <typename BT> struct SpmmArgs {
   int rows_per_unit;               // rb: rows per warp
   int l2_hints;                    // 1: gathered B rows evict_last in L2
   int long_row;                    // rb: rows of >= long_row nonzeros are left to the
-                                   // long-row CTAs (spmm_long.cu); 0: none
+                                   // long-row CTAs or pieces (spmm_long.cu); 0: none
+  // rb_pr: the first piece_cap warps of a row-block launch take the pieces of
+  // the long rows, (row, first nonzero) pairs: piece_count[0] of rows of
+  // several pieces from entry 0, piece_count[1] of one-piece rows from entry
+  // piece_multi.  A piece of several stores its partial row (piece_ld floats)
+  // and counts itself in piece_ctr[first piece of the row * slabs + slab]; the
+  // last piece of a row sums the row's partials in piece order into C.
+  const int2 *__restrict__ pieces;
+  const int *__restrict__ piece_count;
+  unsigned *piece_ctr;
+  float *piece_part;
+  long long piece_cap;
+  long long piece_multi;
+  long long piece_ld;
+  int piece_len;
 };
 
 template <int V> __device__ __forceinline__ void zero(float (&a)[V]) {
@@ -148,6 +162,51 @@ template <int R> __device__ __forceinline__ void put_c(float *p, const float *a,
   }
 }
 
+// The end of a piece of a long row (rb_pr): its R sums of columns c0 .. c0+R-1
+// (`mine`: this lane holds such columns) become the piece's partial row; the
+// piece of the row that counts itself last sums the row's partials in piece
+// order and stores them in C, so the result does not depend on which piece
+// finishes first.  A row of one piece stores directly.
+template <typename BT, int R>
+__device__ __forceinline__ void finish_piece(const SpmmArgs<BT> &a, long long w, int row, int y0,
+                                             int slab, int slabs, const float *acc, bool mine,
+                                             int c0, int lane) {
+  const int rs = __ldg(a.row_ptr + row), re = __ldg(a.row_ptr + row + 1);
+  const int n = (re - rs + a.piece_len - 1) / a.piece_len;
+  float *dst = a.C + (long long)row * a.ldc + c0;
+  if (n == 1) {
+    if (mine) put_c<R>(dst, acc, false);
+    return;
+  }
+  const long long first = w - (y0 - rs) / a.piece_len;
+  if (mine) {
+    float *part = a.piece_part + w * a.piece_ld + c0;
+#pragma unroll
+    for (int k = 0; k < R; ++k) __stcg(part + k, acc[k]);
+  }
+  __threadfence();
+  __syncwarp();
+  unsigned seen = 0;
+  if (lane == 0) seen = atomicAdd(a.piece_ctr + first * slabs + slab, 1u);
+  seen = __shfl_sync(0xffffffffu, seen, 0);
+  if (seen != (unsigned)(n - 1)) return;
+  __threadfence();
+  // every piece of the row has counted itself: the counter is free again (a
+  // later product may reuse the list)
+  if (lane == 0) a.piece_ctr[first * slabs + slab] = 0u;
+  if (mine) {
+    float sum[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) sum[k] = 0.0f;
+    for (int q = 0; q < n; ++q) {
+      const float *part = a.piece_part + (first + q) * a.piece_ld + c0;
+#pragma unroll
+      for (int k = 0; k < R; ++k) sum[k] += __ldcg(part + k);
+    }
+    put_c<R>(dst, sum, false);
+  }
+}
+
 // Rows [lo, lo + rows) of the current column slab of B staged in shared
 // memory (W = G*V values per row): gathers of those rows read the copy.
 template <typename BT> struct Window {
@@ -190,11 +249,24 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
   int x0, x1, y0, y1;
   bool head_split = false, tail_open = false;
   if (ROWS) {
-    const long long r0 = w * a.rows_per_unit;
-    x0 = (int)r0;
-    x1 = (int)min(r0 + a.rows_per_unit, (long long)M);
-    y0 = __ldg(a.row_ptr + x0);
-    y1 = __ldg(a.row_ptr + x1);
+    if (w < a.piece_cap) {
+      // A piece of a long row: its nonzeros [y0, y1), added to the row of C
+      // (zeroed by the list pass) like a merge-path chunk inside one row.
+      if (w < a.piece_multi ? w >= (long long)__ldg(a.piece_count)
+                            : w - a.piece_multi >= (long long)__ldg(a.piece_count + 1))
+        return;
+      const int2 pc = __ldg(a.pieces + w);
+      x0 = x1 = pc.x;
+      y0 = pc.y;
+      y1 = min(pc.y + a.piece_len, __ldg(a.row_ptr + pc.x + 1));
+      head_split = tail_open = true;
+    } else {
+      const long long r0 = (w - a.piece_cap) * a.rows_per_unit;
+      x0 = (int)r0;
+      x1 = (int)min(r0 + a.rows_per_unit, (long long)M);
+      y0 = __ldg(a.row_ptr + x0);
+      y1 = __ldg(a.row_ptr + x1);
+    }
   } else {
     x0 = __ldg(a.part_x + w);
     y0 = __ldg(a.part_y + w);
@@ -205,6 +277,7 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
     tail_open = x1 < M && __ldg(a.row_ptr + x1) < y1;
   }
   const int last = tail_open ? x1 : x1 - 1;  // rows of this unit: x0 .. last
+  const bool piece = ROWS && tail_open;      // a piece of a long row (rb_pr)
 
   // Row ends: lane l holds the end of row wb + l (INT_MAX past the last row).
   int cur = x0, wb = x0;
@@ -222,7 +295,7 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
     }
     const int rend = min(__shfl_sync(FULL, rw, cur - wb), y1);
     if constexpr (ROWS) {
-      if (a.long_row > 0 && rend - cstart >= a.long_row) {
+      if (a.long_row > 0 && !piece && rend - cstart >= a.long_row) {
         // a long row: summed by the long-row CTAs; the batch buffer moves on
         cstart = rend;
         ++cur;
@@ -231,7 +304,7 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
         continue;
       }
     }
-    if (P == 1 || rend - cstart >= LONG) {
+    if (P == 1 || rend - cstart >= LONG || piece) {
       // ---- row `cur` split over the slots --------------------------------
       zero<V>(acc);
       int p0 = cstart;
@@ -330,15 +403,22 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
         // the slots' sums, spread over the lanes: every lane writes its share
         bool owner;
         const int first = fold_slots_scatter<G, V>(acc, lane, owner);
-        if (active && owner) {
-          const bool edge = !ROWS && ((cur == x0 && head_split) || (cur == x1 && tail_open));
+        if (ROWS && piece) {
+          finish_piece<BT, fold_scatter_count<G, V>()>(a, w, cur, y0, slab,
+                                                       (a.N + G * V - 1) / (G * V), acc,
+                                                       active && owner, col0 + first, lane);
+        } else if (active && owner) {
+          const bool edge = (cur == x0 && head_split) || (cur == x1 && tail_open);
           constexpr int R = fold_scatter_count<G, V>();
           put_c<R>(a.C + (long long)cur * a.ldc + col0 + first, acc,
                                             edge);
         }
+      } else if (ROWS && piece) {
+        finish_piece<BT, V>(a, w, cur, y0, slab, (a.N + G * V - 1) / (G * V), acc, active, col0,
+                            lane);
       } else if (active) {
         float *dst = a.C + (long long)cur * a.ldc + col0;
-        if (!ROWS && ((cur == x0 && head_split) || (cur == x1 && tail_open)))
+        if ((cur == x0 && head_split) || (cur == x1 && tail_open))
           atomic_add_c<V>(dst, acc);
         else
           store_c<V>(dst, acc);
@@ -393,7 +473,7 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
       }
       if (incl && active) {
         float *dst = a.C + (long long)r * a.ldc + col0;
-        if (!ROWS && ((r == x0 && head_split) || (r == x1 && tail_open))) {
+        if ((r == x0 && head_split) || (r == x1 && tail_open)) {
           if (mylen > 0) atomic_add_c<V>(dst, acc);
         } else {
           store_c<V>(dst, acc);
@@ -756,7 +836,7 @@ __global__ void __launch_bounds__(kSpmmCta, spmm_min_ctas<V, G, WALK == kWalkRow
     spmm_slot_unit<BT, V, G>(a, w, blockIdx.y, threadIdx.x & 31);
     return;
   }
-  if (w >= a.units) return;  // whole warp leaves together
+  if (w >= a.units + a.piece_cap) return;  // whole warp leaves together
   if (WALK == kWalkFlat)
     spmm_flat_unit<BT, V, G, ROWS>(a, w, blockIdx.y, threadIdx.x & 31);
   else

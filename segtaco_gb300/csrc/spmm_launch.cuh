@@ -28,6 +28,14 @@ template <typename BT> inline SpmmArgs<BT> make_spmm_args(const SpmmLaunch &L) {
   a.rows_per_unit = L.rows_per_unit;
   a.l2_hints = L.l2_hints ? 1 : 0;
   a.long_row = L.long_row;
+  a.pieces = reinterpret_cast<const int2 *>(L.pieces);
+  a.piece_count = L.piece_count;
+  a.piece_ctr = L.piece_ctr;
+  a.piece_part = L.piece_part;
+  a.piece_cap = L.piece_len > 0 ? L.piece_cap : 0;
+  a.piece_multi = L.piece_multi;
+  a.piece_ld = L.piece_ld;
+  a.piece_len = L.piece_len;
   return a;
 }
 
@@ -60,7 +68,8 @@ inline dim3 spmm_grid(const SpmmLaunch &L) {
   const long long W = (long long)L.V * L.G;
   const unsigned slabs = (unsigned)((L.N + W - 1) / W);
   const long long per_warp = L.walk == kWalkSlots ? 32 / L.G : 1;
-  const long long warps = (L.units + per_warp - 1) / per_warp;
+  const long long units = L.units + (L.piece_len > 0 ? L.piece_cap : 0);
+  const long long warps = (units + per_warp - 1) / per_warp;
   long long x = (warps + kSpmmWarps - 1) / kSpmmWarps;
   if (x < 1) x = 1;
   return dim3((unsigned)x, slabs, 1);

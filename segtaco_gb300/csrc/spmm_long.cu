@@ -30,8 +30,17 @@
 // DRAM-bound, and narrower slabs only re-read the row's indices.
 //
 // rb_pr splits a row over the lanes of one warp (segTACO spmm_rb_pr.h:223-375)
-// and meets the same tail; its long rows take the same CTAs, each warp
-// summing a quarter of every stage and the four partials folded at the end.
+// and meets the same tail.  Its long rows become pieces of kPieceLen nonzeros
+// that warps of the row-block launch itself take (spmm_walk_unit), over the
+// same 32-column slabs as the short rows, so both share the slab's L2 working
+// set: long_pieces_list_kernel lists them, each piece stores its partial row
+// in the workspace and the last piece of a row (a counter per row and slab)
+// sums the partial rows in piece order, so the result is the same from run to
+// run.  Measured on GB300 (1M x 1M power law, N = 128): 1.69 ms with the
+// long-row CTAs, 1.58 with pieces at 4 short rows per warp, 1.20 at 32.  The
+// CTAs (each warp summing a quarter of every stage, the four partials folded
+// at the end) remain for the allocation-free entry point, whose fixed scratch
+// cannot hold the partial rows.
 #include <algorithm>
 #include <atomic>
 
@@ -112,6 +121,31 @@ __global__ void long_rows_list_kernel(const int *__restrict__ row_ptr, int M, in
     const int i = atomicAdd(counters + 1, 1);
     if (i < cap_lo) list[cap_hi + i] = (int)r;
   }
+}
+
+// rb_pr: thread per row; a row of >= long_row nonzeros appends its pieces of
+// piece_len nonzeros: several (consecutive entries of the front part, the
+// counters of its first piece cleared, one per column slab) or one (the back
+// part, from entry `multi`).
+__global__ void long_pieces_list_kernel(const int *__restrict__ row_ptr, int M, int long_row,
+                                        int piece_len, int2 *__restrict__ pieces,
+                                        long long multi, long long cap,
+                                        unsigned *__restrict__ ctr, int slabs, int *count) {
+  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= M) return;
+  const int b = __ldg(row_ptr + r);
+  const int len = __ldg(row_ptr + r + 1) - b;
+  if (len < long_row) return;
+  const int n = (len + piece_len - 1) / piece_len;
+  if (n == 1) {
+    const long long i = multi + atomicAdd(count + 1, 1);
+    if (i < cap) pieces[i] = make_int2((int)r, b);
+    return;
+  }
+  const long long i = atomicAdd(count, n);
+  for (int k = 0; k < n && i + k < multi; ++k) pieces[i + k] = make_int2((int)r, b + k * piece_len);
+  if (i < multi)
+    for (int sl = 0; sl < slabs; ++sl) ctr[i * slabs + sl] = 0u;
 }
 
 // One CTA per (column slab of W columns, long row) item at a time; every
@@ -396,6 +430,17 @@ int launch_long_rows_list(const int *row_ptr, int M, long long nnz, int long_row
   long_rows_list_kernel<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(row_ptr, M, long_row, list,
                                                                     cap_hi, cap_lo, counters);
   return check_launch("long_rows_list_kernel");
+}
+
+int launch_long_pieces_list(const int *row_ptr, int M, long long nnz, int long_row, int piece_len,
+                            int slabs, int W, int *pieces, int *count, cudaStream_t s) {
+  SEGTACO_TRY(check_cuda(cudaMemsetAsync(count, 0, 2 * sizeof(int), s), "cudaMemsetAsync"));
+  if (M <= 0) return SEGTACO_OK;
+  const PieceLayout pl = piece_layout(nnz, long_row, piece_len, slabs, W);
+  long_pieces_list_kernel<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(
+      row_ptr, M, long_row, piece_len, reinterpret_cast<int2 *>(pieces), pl.multi, pl.cap,
+      reinterpret_cast<unsigned *>(pieces + pl.ctr), slabs, count);
+  return check_launch("long_pieces_list_kernel");
 }
 
 int launch_spmm_long_rows(const SpmmLaunch &L, const int *list, int *counters, cudaStream_t s) {

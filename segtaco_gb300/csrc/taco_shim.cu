@@ -408,9 +408,12 @@ int run_spmm(const Entry &e, taco_tensor_t *C, taco_tensor_t *A, taco_tensor_t *
     cfg.rows_per_unit = e.rows;
     cfg.items_per_unit = e.items;
     cfg.col_tile = e.col_tile;
-    // Row-block names: long rows to CTAs of their own when the host CSR has any.
+    // Row-block names: long rows out of the row blocks (rb_sr: CTAs of their
+    // own; rb_pr: pieces) when the host CSR has any.
     if ((e.schedule == SEGTACO_RB_SR || e.schedule == SEGTACO_RB_PR) && nnz >= segtaco::kLongRowsMinNnz) {
-      const long long T = segtaco::long_row_threshold(cfg);
+      const long long T = e.schedule == SEGTACO_RB_PR && cfg.items_per_unit <= 0
+                              ? segtaco::kPieceLen
+                              : segtaco::long_row_threshold(cfg);
       for (int r = 0; r < M; ++r)
         if (rp[r + 1] - rp[r] >= T) {
           cfg.flags |= SEGTACO_FLAG_LONG_ROWS;

@@ -172,9 +172,21 @@ def test_workspace_and_heuristic(native_lib):
     assert ws(128, items_per_unit=512, flags=LR) == want(512)
     assert ws(128) == 0
     assert ws(126, flags=LR) == 0
-    c = N.Config.make(schedule="rb_pr", flags=LR)  # rb_pr: the same list
+    # rb_pr: pieces of 512 nonzeros, at most 2 nnz / 512 + 1 of rows of
+    # several pieces (each with a counter per column slab and a partial row)
+    # and nnz / T + 1 one-piece rows; W = 32 columns per slab here, 4 slabs
+    multi = 2 * 2 * 10**7 // 512 + 1  # default threshold for rb_pr: 512
+    cap = multi + 2 * 10**7 // 512 + 1
+    part = (2 * cap + 4 * multi + 63) // 64 * 64
+    c = N.Config.make(schedule="rb_pr", flags=LR)
     assert L.segtaco_spmm_workspace_size(10**6, 10**6, 2 * 10**7, 128, N.F32, C.byref(c),
-                                         C.byref(out)) == N.OK and out.value == want(2048)
+                                         C.byref(out)) == N.OK
+    assert out.value == ((part + multi * 128) * 4 + 255) // 256 * 256 + 256
+    c = N.Config.make(schedule="rb_pr", flags=LR, col_tile=32, vec=4)
+    name = C.create_string_buffer(256)
+    assert L.segtaco_spmm_plan_name(10**6, 10**6, 2 * 10**7, 128, N.F32, None, 128, C.byref(c),
+                                    name, 256) == N.OK
+    assert name.value.decode().startswith("rb_pr pieces ")
     h = N.Config()
     h.schedule = -1
     assert L.segtaco_autotune_heuristic(16384, 16384, 262144, 32, N.F32, 16, C.byref(h)) == N.OK
@@ -184,6 +196,8 @@ def test_workspace_and_heuristic(native_lib):
                                         C.byref(h)) == N.OK
     assert h.schedule == N.EB_PR
     assert (h.col_tile, h.vec) == (32, 8)  # B beyond L2, skewed rows: 8 columns per lane
+    assert h.flags == N.FLAG_L2_HINTS  # ... and the gathered B rows evict_last
+    assert h.items_per_unit == 512
     h.schedule = -1
     assert L.segtaco_autotune_heuristic(262144, 262144, 19135456, 64, N.F32, 73,
                                         C.byref(h)) == N.OK
@@ -203,11 +217,26 @@ def test_workspace_and_heuristic(native_lib):
                                             C.byref(h)) == N.OK
         assert h.schedule == sched and h.col_tile == tile and h.vec == 0
         assert h.items_per_unit == items and h.flags == flags
-    for max_len, flags in ((2047, 0), (2048, N.FLAG_LONG_ROWS), (-1, 0)):  # rows known short
-        h.schedule = N.RB_PR                                             # or unknown: none
+    # rb_pr: long rows (pieces) from 512 nonzeros, then 32 short rows per warp;
+    # rows known short or unknown: none (unknown: not skewed, no L2 hints)
+    H, LR = N.FLAG_L2_HINTS, N.FLAG_LONG_ROWS
+    for max_len, flags, rows, items in ((511, H, 4, 2048), (512, LR | H, 32, 512),
+                                        (48679, LR | H, 32, 512), (-1, 0, 4, 2048)):
+        h.schedule = N.RB_PR
         assert L.segtaco_autotune_heuristic(10**6, 10**6, 2 * 10**7, 128, N.F32, max_len,
                                             C.byref(h)) == N.OK
-        assert h.flags == flags
+        assert (h.flags, h.rows_per_unit, h.items_per_unit) == (flags, rows, items), max_len
+    h.schedule = N.RB_PR  # long rows under a mean of 73 nonzeros per row: 4 rows per warp
+    assert L.segtaco_autotune_heuristic(262144, 262144, 19135456, 64, N.F32, 580,
+                                        C.byref(h)) == N.OK
+    assert h.flags == N.FLAG_LONG_ROWS and h.rows_per_unit == 4
+    # small products: merge-path chunks shrink until the grid holds 4,096 of
+    # them (16,384 rows + 262,144 nonzeros: 64 items); rb_sr 2 rows per warp
+    for sched, items, rows in ((N.EB_PR, 64, 1), (N.EB_SR, 64, 1), (N.RB_SR, 2048, 2)):
+        h.schedule = sched
+        assert L.segtaco_autotune_heuristic(16384, 16384, 262144, 32, N.F32, 16,
+                                            C.byref(h)) == N.OK
+        assert (h.items_per_unit, h.rows_per_unit) == (items, rows), sched
     h.schedule = N.RB_SR  # bf16 too: 128-column slabs (8-byte lanes) from 1M nonzeros
     assert L.segtaco_autotune_heuristic(10**6, 10**6, 2 * 10**7, 128, N.BF16, 48679,
                                         C.byref(h)) == N.OK

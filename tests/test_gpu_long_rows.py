@@ -7,8 +7,10 @@ storage order, so the result must be bit-identical to the one-warp walk
 (spmm_rb_sr.h:187-243): across thresholds, widths (one and several column
 slabs, widths the 16-byte copies cannot take), bf16 B, unit values, offset B,
 the partition-ready split, and graph capture (the allocation-free entry point:
-test_zz_no_alloc.py).  rb_pr: four warps' partial sums folded, within the
-FP64 bound of 1e-5 and bit-identical from run to run."""
+test_zz_no_alloc.py).  rb_pr: the long rows are pieces of 512 nonzeros in
+the row-block launch (over the same column slabs), whose partial rows the
+last piece of each row sums in piece order: within the FP64 bound of 1e-5 and
+bit-identical from run to run."""
 import numpy as np
 import pytest
 import torch
@@ -159,3 +161,51 @@ def test_rb_pr_thresholds_and_bf16(cuda, A, threshold):
     B = synth.dense(A.K, 128, seed=61)
     got = run(dev(A), torch.from_numpy(B).cuda(), 128, "rb_pr", items_per_unit=threshold)
     assert_spmm_close(got, A, B)
+
+
+def test_rb_pr_pieces_partition_ready_and_graph(cuda, A):
+    """rb_pr's long rows as pieces of the row-block launch: the plan names
+    them; a list made once serves repeated products (each row's piece
+    counters return to zero when its last piece has summed the partial rows),
+    and a captured graph replays; every result is bit-identical (the partial
+    rows are summed in piece order, whichever piece finishes last)."""
+    B = synth.dense(A.K, 128, seed=62)
+    Ad, Bd = dev(A), torch.from_numpy(B).cuda()
+    cfg = N.Config.make(schedule="rb_pr", flags=N.FLAG_LONG_ROWS)
+    assert ops.plan_name(Ad, Bd, cfg).startswith("rb_pr pieces ")
+    ws = torch.empty(ops.spmm_workspace_size(Ad, 128, N.F32, cfg), dtype=torch.uint8,
+                     device="cuda")
+    C_ = torch.full((A.M, 128), float("nan"), device="cuda")
+    ops.spmm_partition(Ad, C_, cfg, ws)
+    ready = N.Config.make(schedule="rb_pr", flags=N.FLAG_LONG_ROWS | N.FLAG_PARTITION_READY)
+    first = None
+    for _ in range(3):
+        C_.fill_(float("nan"))
+        ops.spmm(Ad, Bd, C_out=C_, config=ready, workspace=ws)
+        torch.cuda.synchronize()
+        got = C_.cpu().numpy()
+        if first is None:
+            first = got
+            assert_spmm_close(got, A, B)
+        assert np.array_equal(got, first)
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        ops.spmm(Ad, Bd, C_out=C_, config=cfg, workspace=ws)
+    for _ in range(2):
+        C_.fill_(float("nan"))
+        g.replay()
+        torch.cuda.synchronize()
+        assert np.array_equal(C_.cpu().numpy(), first)
+
+
+@pytest.mark.parametrize("threshold,n", [(1, 64), (300, 40), (513, 128), (1024, 96)])
+def test_rb_pr_pieces_one_and_several(cuda, A, threshold, n):
+    """Thresholds at and around the piece length (512): rows of one piece
+    (stored directly) beside rows of several, ragged widths; identical reruns."""
+    B = synth.dense(A.K, n, seed=63 + n)
+    Ad, Bd = dev(A), torch.from_numpy(B).cuda()
+    cfg = dict(items_per_unit=threshold)
+    got = run(Ad, Bd, n, "rb_pr", **cfg)
+    assert_spmm_close(got, A, B)
+    assert np.array_equal(got, run(Ad, Bd, n, "rb_pr", **cfg))
