@@ -158,6 +158,12 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
                              : (k == 1604 || k == 804 || k == 808);
     if (ok) plan->walk = 3;
   }
+  // eb_sr with 8-byte lanes (bf16 over 128-column slabs, fp32 over 64): the
+  // sequential walk with staged indices (spmm_seq_unit), unless a walk is
+  // forced.
+  if (schedule == SEGTACO_EB_SR && G == 32 && !plan->use_tma && plan->walk == 0 &&
+      !(c.flags & (SEGTACO_FLAG_ROW_WALK | SEGTACO_FLAG_FLAT_WALK)) && V * esz == 8)
+    plan->walk = 4;
   plan->rows_per_unit = c.rows_per_unit > 0 ? c.rows_per_unit : 1;
   plan->items_per_unit = 0;
   plan->nchunks = (M + plan->rows_per_unit - 1) / plan->rows_per_unit;  // rb: row blocks

@@ -808,10 +808,129 @@ __device__ __forceinline__ void spmm_slot_unit(const SpmmArgs<BT> &a, long long 
   }
 }
 
+// Sequential walk of a merge-path chunk for 8-byte lanes (eb_sr with bf16 B
+// over 128-column slabs, or fp32 over 64): the warp is one slot and walks the
+// chunk's nonzeros in storage order, every column of a row one fmaf chain, as
+// the flat walk does for 16-byte lanes.  Instead of two shuffles per gather
+// (index and value), the chunk's indices and values are staged in shared
+// memory by coalesced loads (kSeqStage at a time) and each step reads four of
+// them with one broadcast 16-byte shared load per array, then issues U
+// gathers before the first multiply-add.  Control flow is warp-uniform: row
+// ends come from a window of 32 row ends in the lanes.  A row cut by a chunk
+// edge is zeroed by the partition kernel and receives red.global.add from each
+// chunk holding part of it.  Measured on GB300 (1M x 1M power law, N = 128):
+// bf16 eb_sr 0.840 -> 0.819 ms against the row walk, fp32 at 64 columns 1.500
+// -> 1.472 ms (the flat walk over 128 columns stays the fp32 default, 1.434
+// ms).  With 4-byte lanes (one fp32 column per lane, 32-column slabs) it took
+// 2.55 ms at 16 gathers in flight (32 spill): a gather then brings only 128
+// bytes per warp, so the walk is bound by its per-position work.
+constexpr int kSeqStage = 512;
+template <typename BT, int V> __host__ __device__ constexpr int seq_loads() { return 8; }
+template <typename BT, int V>
+__device__ __forceinline__ void spmm_seq_unit(const SpmmArgs<BT> &a, long long w, int slab,
+                                              int lane, int *__restrict__ cs,
+                                              float *__restrict__ vs) {
+  constexpr int U = seq_loads<BT, V>();
+  using D = Dense<BT, V>;
+  const unsigned FULL = 0xffffffffu;
+  const int M = a.M;
+  const int col0 = slab * (32 * V) + lane * V;
+  const bool active = col0 < a.N;
+  const uint64_t pol = l2_policy(a.l2_hints);
+  const BT *Bc = a.B + (active ? col0 : 0);  // lanes past N load column 0, never store
+  const unsigned ldb = (unsigned)a.ldb;
+
+  const int x0 = __ldg(a.part_x + w), y0 = __ldg(a.part_y + w);
+  const int x1 = __ldg(a.part_x + w + 1), y1 = __ldg(a.part_y + w + 1);
+  // Row x0 began in an earlier chunk; row x1 holds nonzeros here and ends later.
+  const bool head_split = x0 < M && __ldg(a.row_ptr + x0) < y0;
+  const bool tail_open = x1 < M && __ldg(a.row_ptr + x1) < y1;
+  int wb = x0;  // lane l: end of row wb + l
+  int rw = wb + lane < M ? __ldg(a.row_ptr + wb + 1 + lane) : INT_MAX;
+  auto row_end = [&](int r) -> int {
+    while (r - wb >= 32) {
+      wb += 32;
+      rw = wb + lane < M ? __ldg(a.row_ptr + wb + 1 + lane) : INT_MAX;
+    }
+    return __shfl_sync(FULL, rw, r - wb);
+  };
+  float acc[V];
+  zero<V>(acc);
+  auto flush = [&](int r) {
+    if (active) {
+      float *dst = a.C + (long long)r * a.ldc + col0;
+      if ((r == x0 && head_split) || (r == x1 && tail_open))
+        atomic_add_c<V>(dst, acc);
+      else
+        store_c<V>(dst, acc);
+    }
+    zero<V>(acc);
+  };
+  int row = x0;
+  int rend = row_end(row);  // INT_MAX past the last row
+  int base = 0, lim = -1;  // staged nonzeros [base, lim), base a multiple of 4
+  int p = y0;
+  while (p < y1) {
+    if (p >= lim) {
+      __syncwarp();
+      base = p & ~3;
+      lim = min(base + kSeqStage, y1);
+      for (int k = lane; k < lim - base; k += 32) {
+        cs[k] = ld_stream(a.col + base + k);
+        vs[k] = ld_val(a.val, base + k);
+      }
+      __syncwarp();
+    }
+    // Positions g .. g+U-1 of this step (g a multiple of 4); those in [p, end)
+    // are this chunk's, the others load B row 0 (a cache hit) and are unused.
+    const int g = p & ~3;
+    const int end = min(g + U, lim);
+    const int o = g - base;
+    typename D::raw_t b[U];
+#pragma unroll
+    for (int j = 0; j < U / 4; ++j) {
+      const int4 c4 = *reinterpret_cast<const int4 *>(cs + o + 4 * j);
+      const int cc[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int pos = g + 4 * j + k;
+        const int col = pos >= p && pos < end ? cc[k] : 0;
+        b[4 * j + k] = D::load(Bc + (size_t)(unsigned)col * ldb, pol);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < U / 4; ++j) {
+      const float4 v4 = *reinterpret_cast<const float4 *>(vs + o + 4 * j);
+      const float vv[4] = {v4.x, v4.y, v4.z, v4.w};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int pos = g + 4 * j + k;
+        if (pos >= p && pos < end) {
+          while (pos >= rend) {  // rows ending before this position (empty ones too)
+            flush(row);
+            ++row;
+            rend = row_end(row);
+          }
+#pragma unroll
+          for (int v = 0; v < V; ++v) acc[v] = fmaf(vv[k], D::get(b[4 * j + k], v), acc[v]);
+        }
+      }
+    }
+    p = end;
+  }
+  // Rows that end inside the chunk after its last nonzero (empty or not), then
+  // the row still open at the chunk's end.
+  while (row < x1) {
+    flush(row);
+    ++row;
+  }
+  if (tail_open) flush(x1);
+}
+
 // Walks of a unit: the row walk with 4 or 8 loads in flight per lane, the
-// flat walk, or the slot walk over merge-path chunks (chosen by the planner,
-// api.cu).
-constexpr int kWalkRows = 0, kWalkRowsDeep = 1, kWalkFlat = 2, kWalkSlots = 3;
+// flat walk, the slot walk or the sequential walk over merge-path chunks
+// (chosen by the planner, api.cu).
+constexpr int kWalkRows = 0, kWalkRowsDeep = 1, kWalkFlat = 2, kWalkSlots = 3, kWalkSeq = 4;
 
 // CTAs of the SpMM kernels: 4 warps each, so a CTA that finishes early frees
 // its slot soon (warps of a CTA walk units of uneven cost).  32 warps per SM
@@ -834,6 +953,14 @@ __global__ void __launch_bounds__(kSpmmCta, spmm_min_ctas<V, G, WALK == kWalkRow
   if constexpr (WALK == kWalkSlots) {  // a.units chunks, 32 / G per warp
     if (w * (32 / G) >= a.units) return;
     spmm_slot_unit<BT, V, G>(a, w, blockIdx.y, threadIdx.x & 31);
+    return;
+  }
+  if constexpr (WALK == kWalkSeq) {  // merge-path chunks, one per warp
+    __shared__ __align__(16) int s_col[kSpmmWarps][kSeqStage + seq_loads<BT, V>()];
+    __shared__ __align__(16) float s_val[kSpmmWarps][kSeqStage + seq_loads<BT, V>()];
+    if (w >= a.units) return;
+    const int wi = threadIdx.x / 32;
+    spmm_seq_unit<BT, V>(a, w, blockIdx.y, threadIdx.x & 31, s_col[wi], s_val[wi]);
     return;
   }
   if (w >= a.units + a.piece_cap) return;  // whole warp leaves together

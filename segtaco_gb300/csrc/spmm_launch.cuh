@@ -121,6 +121,26 @@ inline dim3 spmm_grid(const SpmmLaunch &L) {
     }                                                                                    \
   }
 
+// Sequential-walk variants (merge-path chunks, one 32-lane slot): 8-byte lanes.
+#define SEGTACO_SEQ_CASE(BT, V)                                                          \
+  case V:                                                                                \
+    launch_seg(spmm_seg_kernel<BT, V, 32, false, kWalkSeq>, grid, s, a, L.carveout);     \
+    break;
+#define SEGTACO_SEQ_CASES(BT)                                                            \
+  if constexpr (sizeof(BT) == 4) {                                                       \
+    switch (L.V) {                                                                       \
+      SEGTACO_SEQ_CASE(BT, 2)                                                            \
+      default:                                                                           \
+        return set_error(SEGTACO_EUNSUPPORTED, "sequential walk: no variant V=%d", L.V); \
+    }                                                                                    \
+  } else {                                                                               \
+    switch (L.V) {                                                                       \
+      SEGTACO_SEQ_CASE(BT, 4)                                                            \
+      default:                                                                           \
+        return set_error(SEGTACO_EUNSUPPORTED, "sequential walk: no variant V=%d", L.V); \
+    }                                                                                    \
+  }
+
 // Defines int NAME(const SpmmLaunch&, cudaStream_t) for one (dtype, unit kind).
 #define SEGTACO_DEFINE_SPMM_LAUNCHER(NAME, BT, VG_LIST, ROWS)                             \
   namespace segtaco {                                                                     \
@@ -130,6 +150,10 @@ inline dim3 spmm_grid(const SpmmLaunch &L) {
     if constexpr (!ROWS) {                                                                \
       if (L.walk == kWalkSlots) {                                                         \
         SEGTACO_SLOT_CASES(BT)                                                            \
+        return check_launch(#NAME);                                                       \
+      }                                                                                   \
+      if (L.walk == kWalkSeq) {                                                           \
+        SEGTACO_SEQ_CASES(BT)                                                             \
         return check_launch(#NAME);                                                       \
       }                                                                                   \
     }                                                                                     \
