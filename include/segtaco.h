@@ -88,15 +88,25 @@ extern "C" {
                                       0 = 64) in merge order, each row of a chunk
                                       one sequential chain; rows cut by chunk
                                       edges are combined by atomics */
-#define SEGTACO_FLAG_WINDOW 128u /* rb schedules: each CTA of 4 * rows_per_unit rows
-                                     stages the B rows [i0 - H, i1 + H) of its column
-                                     slab in shared memory with one TMA tensor copy
-                                     and gathers rows inside that window from it
-                                     (H = items_per_unit; 0 = 32); for matrices
-                                     whose nonzeros lie near the diagonal.  Needs B
-                                     16-byte aligned, ldb * element size a multiple
-                                     of 16 and 4 * rows_per_unit + 2H <= 256;
-                                     otherwise ignored.  Not with LONG_ROWS     */
+#define SEGTACO_FLAG_WINDOW 128u /* rb schedules, matrices whose nonzeros lie
+                                     near the diagonal (H = items_per_unit; 0 =
+                                     32).  rb_pr with N >= 64 (a multiple of 16),
+                                     C 16-byte aligned and ldc a multiple of 4:
+                                     the band kernel -- 32-row blocks with B rows
+                                     [i0 - H, i0 + 32 + H) of a 64-column slab in
+                                     shared memory (one TMA tensor copy), the
+                                     block's in-band nonzeros as a dense tile, 4 x
+                                     4 register tiles, off-band nonzeros gathered;
+                                     32 + 2H <= 256.  Otherwise each CTA of 4 *
+                                     rows_per_unit rows stages B rows [i0 - H,
+                                     i1 + H) of its slab and gathers rows inside
+                                     that window from it (4 * rows_per_unit + 2H
+                                     <= 256).  Needs B 16-byte aligned and ldb *
+                                     element size a multiple of 16; otherwise
+                                     ignored.  Not with LONG_ROWS.
+                                     segtaco_autotune_heuristic reads the bit as
+                                     "rows lie near the diagonal" and keeps it
+                                     for rb_pr's band kernel                    */
 
 /* Tuning knobs.  Zero in a field means "choose automatically". */
 typedef struct segtaco_config {

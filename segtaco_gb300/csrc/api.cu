@@ -211,8 +211,18 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
     }
   }
   plan->window_halo = -1;
-  if ((c.flags & SEGTACO_FLAG_WINDOW) && plan->long_row == 0 && !plan->use_tma && nnz > 0 &&
-      K > 0 &&
+  plan->band_halo = -1;
+  if ((c.flags & SEGTACO_FLAG_WINDOW) && schedule == SEGTACO_RB_PR && plan->long_row == 0 &&
+      !plan->use_tma && nnz > 0 && K > 0 && N >= 64 && N % 16 == 0 &&
+      ((uintptr_t)B % 16) == 0 && (ldb * esz) % 16 == 0 && ((uintptr_t)C % 16) == 0 &&
+      ldc % 4 == 0) {
+    // rb_pr on a banded matrix: 32-row blocks with the band of A as a dense
+    // tile and B's window of 32 + 2H rows by TMA (spmm_band_kernel).
+    const long long H = c.items_per_unit > 0 ? c.items_per_unit : 32;
+    if (32 + 2 * H <= 256) plan->band_halo = (int)H;
+  }
+  if ((c.flags & SEGTACO_FLAG_WINDOW) && plan->band_halo < 0 && plan->long_row == 0 &&
+      !plan->use_tma && nnz > 0 && K > 0 &&
       (schedule == SEGTACO_RB_SR || schedule == SEGTACO_RB_PR) && plan->walk != 2) {
     // TMA needs B 16-byte aligned and its row pitch a multiple of 16 bytes;
     // the window's rows (4 per-warp row blocks plus two halos) fit one box.
@@ -259,11 +269,13 @@ int run_spmm_planned(const SpmmPlan &plan, int M, int K, long long nnz, const in
   L.walk = plan.walk;
   L.no_fork = plan.no_fork;
   L.window_halo = plan.window_halo;
+  L.band_halo = plan.band_halo;
   const bool bf16 = b_dtype == SEGTACO_BF16;
   switch (plan.schedule) {
     case SEGTACO_RB_SR:
     case SEGTACO_RB_PR:
       if (L.use_tma) return bf16 ? launch_spmm_tma_bf16(L, true, s) : launch_spmm_tma_f32(L, true, s);
+      if (plan.band_halo >= 0) return launch_spmm_band(L, s);
       if (plan.window_halo >= 0) return launch_spmm_window(L, s);
       if (plan.long_row > 0 && plan.piece_len > 0) {
         L.long_row = plan.long_row;
@@ -425,13 +437,19 @@ int segtaco_autotune_heuristic(int32_t M, int32_t K, int64_t nnz, int32_t N, int
   // / 1.687).
   if (!sequential && esz == 4 && bbytes > 48e6 && skewed) cfg->flags |= SEGTACO_FLAG_L2_HINTS;
   // Rows known to lie near the diagonal (the caller's segtaco_band_stats):
-  // the staged B window is NOT chosen.  Measured on GB300, banded 262,144
-  // rows, N = 64: the row-block kernel's gathers of the band already hit L1,
-  // and shared-memory reads of the window go through the same load/store
-  // data pipe, so the window (rows_per_unit 16, halo 32) took 0.373 ms fp32
-  // against 0.248 ms for the plain row blocks with one 64-column slab.  The
-  // bit is accepted so that callers may pass their band statistics.
-  (void)banded;
+  // rb_pr takes the band kernel (32-row blocks, the band of A as a dense tile,
+  // B's window by TMA, 4 x 4 register tiles; spmm_window.cu) with a halo of
+  // 32.  Measured on GB300, banded-plus-random 262,144 rows (half band 32, 8
+  // off-band nonzeros per row): fp32 N = 64 0.2465 -> 0.2325 ms, bf16 B
+  // 0.2323 -> 0.1725 ms, fp32 N = 128 0.650 -> 0.455 ms (halo 16: 0.61 ms,
+  // 48: 0.29 ms at fp32 N = 64).  The staged window for the row-block walk
+  // (still one gathered B slice per nonzero, from shared memory instead of
+  // L1) measured slower than the plain row blocks (0.373 vs 0.248 ms) and is
+  // not chosen; rb_sr keeps the plain row blocks.
+  if (banded && schedule == SEGTACO_RB_PR && !long_rows && N >= 64 && N % 16 == 0) {
+    cfg->flags |= SEGTACO_FLAG_WINDOW;
+    cfg->items_per_unit = 32;
+  }
   return SEGTACO_OK;
 }
 
@@ -443,12 +461,14 @@ int segtaco_spmm_plan_name(int32_t M, int32_t K, int64_t nnz, int32_t N, int32_t
   SEGTACO_TRY(plan_spmm(M, K, nnz, N, b_dtype, ldb, N, B, nullptr, cfg, &plan));
   static const char *sched[] = {"rb_sr", "rb_pr", "eb_sr", "eb_pr"};
   const char *kernel = plan.use_tma         ? "tma_ring"
+                       : plan.band_halo >= 0   ? "band"
                        : plan.window_halo >= 0 ? "window"
                        : plan.long_row > 0 ? (plan.piece_len > 0 ? "pieces" : "long_rows")
                        : (plan.schedule >= SEGTACO_EB_SR) ? "chunks" : "rows";
   snprintf(out, len, "%s %s V=%d G=%d W=%d slabs=%d walk=%d halo=%d rows_per_unit=%lld",
            sched[plan.schedule], kernel, plan.V, plan.G, plan.W, plan.slabs, plan.walk,
-           plan.window_halo, (long long)plan.rows_per_unit);
+           plan.band_halo >= 0 ? plan.band_halo : plan.window_halo,
+           (long long)plan.rows_per_unit);
   return SEGTACO_OK;
 }
 

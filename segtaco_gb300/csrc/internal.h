@@ -81,6 +81,7 @@ struct SpmmLaunch {
                                // stream or events are created)
   int window_halo = -1;        // >= 0: rb rows with B rows [i0 - halo, i1 + halo) of each
                                // row block staged by TMA (spmm_window.cu)
+  int band_halo = -1;          // >= 0: rb_pr banded row blocks (spmm_band_kernel)
   // rb_pr long rows as pieces of piece_len nonzeros in the row-block launch
   // (spmm_long.cu): (row, first nonzero) pairs, their count, the list capacity.
   int piece_len = 0;
@@ -104,6 +105,9 @@ int launch_spmm_tma_bf16(const SpmmLaunch &L, bool rows, cudaStream_t s);
 int tma_status_ptr(int **out);
 // Row blocks with their B window staged in shared memory (rb only).
 int launch_spmm_window(const SpmmLaunch &L, cudaStream_t s);
+// Banded row blocks of rb_pr: 32 rows x 64 columns per CTA, the band of A as a
+// dense tile, B's band window by TMA (spmm_window.cu).
+int launch_spmm_band(const SpmmLaunch &L, cudaStream_t s);
 bool window_variant_exists(int dtype, int V, int G);
 int launch_band_stats(const int *row_ptr, const int *col, int M, int K, int halo,
                       unsigned long long *out, cudaStream_t s);
@@ -122,6 +126,7 @@ struct SpmmPlan {
   int long_row;              // rb: long-row threshold (0: every row in the row-block kernel)
   bool no_fork = false;      // rb long rows: no side stream (segtaco_spmm_noalloc)
   int window_halo = -1;      // rb: >= 0 stages each row block's B window (spmm_window.cu)
+  int band_halo = -1;        // rb_pr: >= 0 banded row blocks with a dense band tile
   int piece_len = 0;         // rb_pr: long rows split into pieces of this many nonzeros
   long long px_entries;      // int32 entries of the first workspace array (eb: chunk-edge
                              // rows; rb long rows: the list of long rows)

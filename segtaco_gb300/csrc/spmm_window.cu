@@ -101,6 +101,216 @@ __global__ void __launch_bounds__(kSpmmCta, window_min_ctas<BT, V, G>())
   spmm_walk_unit<BT, V, G, true, false, true>(a, w, blockIdx.y, threadIdx.x & 31, wv);
 }
 
+// ---------------------------------------------------------------------------
+// Banded row blocks for rb_pr (SEGTACO_FLAG_WINDOW with a parallel reduction).
+//
+// On a banded matrix the plain row blocks deliver each nonzero's 64-column B
+// slice to registers (256 bytes for 64 multiply-adds), and that load/store
+// data pipe is their bound; the window kernel above only moves the same bytes
+// from shared memory instead of L1.  Here B values are reused from registers:
+// a CTA owns kBandRows = 32 consecutive rows and a slab of 64 columns, brings
+// the band window B[jw0 .. jw0 + win) x slab (win = 32 + 2H rows around the
+// diagonal, column i0 * K / M of its first row) into shared memory with one
+// TMA tensor copy, and scatters its rows' in-window nonzeros into a dense
+// tile At[win][32] (row pitch kBandPitch = 36 floats: 16-byte aligned, and
+// the scatter's consecutive columns of one row spread over 8 banks).  Thread
+// (rb, cb) then keeps rows 4rb .. 4rb+3 x columns 4cb .. 4cb+3 in registers
+// and, for every window row j, reads At[j][4rb .. 4rb+3] and B[j][4cb ..
+// 4cb+3] (two 16-byte shared loads) for 16 multiply-adds: 2 bytes to
+// registers per multiply-add.  The tile holds zeros where a row has no
+// nonzero (win steps per row instead of ~2H + 1 nonzeros), and the summation
+// order within a row differs from the storage order, which the parallel
+// reduction allows; duplicate entries of a row add up in the tile.
+//
+// The scatter reads the block's nonzeros (contiguous in A) coalesced, finding
+// each one's row among the 33 staged row starts; off-band nonzeros (outside
+// the window) go to a per-row list of kBandList entries, and each thread
+// gathers its 4 columns of them from global memory, 8 at a time (a row with
+// more walks its nonzeros in global memory instead).  The TMA wait is bounded
+// as in the window kernel (SEGTACO_ETIMEOUT, rows left unwritten).
+constexpr int kBandRows = 32;
+constexpr int kBandCols = 64;
+constexpr int kBandList = 16;
+constexpr int kBandPitch = 36;
+
+// Four consecutive B values as floats: from shared memory, or from global
+// memory through the read-only path.
+template <typename BT> __device__ __forceinline__ float4 band_b4(const BT *p) {
+  if constexpr (sizeof(BT) == 4) {
+    return *reinterpret_cast<const float4 *>(p);
+  } else {
+    const uint2 x = *reinterpret_cast<const uint2 *>(p);
+    return make_float4(bf16lo(x.x), bf16hi(x.x), bf16lo(x.y), bf16hi(x.y));
+  }
+}
+template <typename BT> __device__ __forceinline__ float4 band_b4_global(const BT *p) {
+  if constexpr (sizeof(BT) == 4) {
+    return __ldg(reinterpret_cast<const float4 *>(p));
+  } else {
+    const uint2 x = __ldg(reinterpret_cast<const uint2 *>(p));
+    return make_float4(bf16lo(x.x), bf16hi(x.x), bf16lo(x.y), bf16hi(x.y));
+  }
+}
+__device__ __forceinline__ void band_fma4(float (&acc)[4], float x, const float4 &b) {
+  acc[0] = fmaf(x, b.x, acc[0]);
+  acc[1] = fmaf(x, b.y, acc[1]);
+  acc[2] = fmaf(x, b.z, acc[2]);
+  acc[3] = fmaf(x, b.w, acc[3]);
+}
+
+// Shared-memory layout of a band CTA (byte offsets; win = window rows).
+struct BandSmem {
+  size_t at, rp, cnt, lcol, lval, bar, bytes;
+};
+template <typename BT> __host__ __device__ inline BandSmem band_smem(int win) {
+  BandSmem m;
+  size_t o = ((size_t)win * kBandCols * sizeof(BT) + 127) & ~size_t(127);  // B window first
+  m.at = o;
+  o += (size_t)win * kBandPitch * 4;
+  m.rp = o;
+  o += (kBandRows + 1) * 4;
+  m.cnt = o;
+  o += kBandRows * 4;
+  m.lcol = o;
+  o += kBandRows * kBandList * 4;
+  m.lval = o;
+  o += kBandRows * kBandList * 4;
+  m.bar = (o + 7) & ~size_t(7);
+  m.bytes = m.bar + 8;
+  return m;
+}
+
+template <typename BT>
+__global__ void __launch_bounds__(kSpmmCta)
+    spmm_band_kernel(SpmmArgs<BT> a, const __grid_constant__ CUtensorMap tm, int halo,
+                     int *status) {
+  const int win = kBandRows + 2 * halo;
+  const BandSmem L = band_smem<BT>(win);
+  extern __shared__ __align__(128) unsigned char smem[];
+  BT *bw = reinterpret_cast<BT *>(smem);  // [win][kBandCols]
+  float *at = reinterpret_cast<float *>(smem + L.at);  // [win][kBandPitch]
+  int *rp = reinterpret_cast<int *>(smem + L.rp);
+  int *cnt = reinterpret_cast<int *>(smem + L.cnt);
+  int *lcol = reinterpret_cast<int *>(smem + L.lcol);
+  float *lval = reinterpret_cast<float *>(smem + L.lval);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L.bar);
+  const int t = threadIdx.x;
+  const int M = a.M;
+  const int i0 = blockIdx.x * kBandRows;
+  const int jw0 = (int)((long long)i0 * a.K / M) - halo;
+  const uint32_t b = sm_u32(bar);
+  if (t == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (int e = t; e < win * kBandPitch; e += kSpmmCta) at[e] = 0.0f;
+  if (t <= kBandRows) rp[t] = __ldg(a.row_ptr + min(i0 + t, M));
+  if (t < kBandRows) cnt[t] = 0;
+  __syncthreads();
+  if (t == 0) {
+    const uint32_t bytes = (uint32_t)((size_t)win * kBandCols * sizeof(BT));
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes)
+                 : "memory");
+    // x = the slab's first column (a multiple of 64 elements), y = the
+    // window's first row (negative at the top edge: zero-filled)
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cta.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(sm_u32(bw)),
+        "l"(&tm), "r"((int)(blockIdx.y * kBandCols)), "r"(jw0), "r"(b)
+        : "memory");
+  }
+  // Scatter the block's nonzeros rp[0] .. rp[32]-1, four per thread per pass
+  // (loads first, then the row searches and shared-memory updates).
+  const int k_end = rp[kBandRows];
+  for (int k0 = rp[0] + t; k0 < k_end; k0 += 4 * kSpmmCta) {
+    int cj[4];
+    float cv[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int k = k0 + q * kSpmmCta;
+      cj[q] = k < k_end ? __ldg(a.col + k) : 0;
+      cv[q] = k < k_end ? ld_val(a.val, k) : 0.0f;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int k = k0 + q * kSpmmCta;
+      if (k < k_end) {
+        int r = 0;  // the last row whose start is <= k
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1)
+          if (r + step <= kBandRows - 1 && rp[r + step] <= k) r += step;
+        const unsigned d = (unsigned)(cj[q] - jw0);
+        if (d < (unsigned)win) {
+          atomicAdd(at + d * kBandPitch + r, cv[q]);
+        } else {
+          const int slot = atomicAdd(cnt + r, 1);
+          if (slot < kBandList) {
+            lcol[r * kBandList + slot] = cj[q];
+            lval[r * kBandList + slot] = cv[q];
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (!window_wait(b)) {
+    if (t == 0) atomicExch(status, SEGTACO_ETIMEOUT);
+    window_wait(b);  // the copy may still land: wait for it once more, bounded
+    return;
+  }
+  const int rb = t >> 4, cb = t & 15;
+  const int c0 = blockIdx.y * kBandCols + 4 * cb;  // this thread's first column
+  if (c0 >= a.N) return;                           // N is a multiple of 16
+  float acc[4][4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.0f;
+  const float *acol = at + 4 * rb;
+  const BT *bcol = bw + 4 * cb;
+#pragma unroll 4
+  for (int j = 0; j < win; ++j) {
+    const float4 x = *reinterpret_cast<const float4 *>(acol + j * kBandPitch);
+    const float4 bv = band_b4<BT>(bcol + j * kBandCols);
+    band_fma4(acc[0], x.x, bv);
+    band_fma4(acc[1], x.y, bv);
+    band_fma4(acc[2], x.z, bv);
+    band_fma4(acc[3], x.w, bv);
+  }
+  // Off-band nonzeros of the thread's four rows, from global memory.
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int r = 4 * rb + q;
+    const int n = cnt[r];
+    if (n <= kBandList) {
+      for (int e0 = 0; e0 < n; e0 += 8) {
+        float4 g[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          const int ee = e0 + e < n ? e0 + e : e0;
+          g[e] = band_b4_global<BT>(a.B + (size_t)(unsigned)lcol[r * kBandList + ee] * a.ldb + c0);
+        }
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+          if (e0 + e < n) band_fma4(acc[q], lval[r * kBandList + e0 + e], g[e]);
+      }
+    } else {
+      // more off-band nonzeros than the list holds: walk the row
+      for (int k = rp[r]; k < rp[r + 1]; ++k) {
+        const int j = __ldg(a.col + k);
+        if ((unsigned)(j - jw0) >= (unsigned)win)
+          band_fma4(acc[q], ld_val(a.val, k),
+                    band_b4_global<BT>(a.B + (size_t)(unsigned)j * a.ldb + c0));
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int i = i0 + 4 * rb + q;
+    if (i < M)
+      __stcs(reinterpret_cast<float4 *>(a.C + (long long)i * a.ldc + c0),
+             make_float4(acc[q][0], acc[q][1], acc[q][2], acc[q][3]));
+  }
+}
+
 // cuTensorMapEncodeTiled from the driver, looked up once.
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   static std::once_flag once;
@@ -183,6 +393,46 @@ template <typename BT> int launch_window(const SpmmLaunch &L, cudaStream_t s) {
   return set_error(SEGTACO_EUNSUPPORTED, "window: no variant V=%d G=%d", L.V, L.G);
 }
 
+template <typename BT> int launch_band_typed(const SpmmLaunch &L, cudaStream_t s) {
+  const int win = kBandRows + 2 * L.band_halo;
+  if (L.band_halo < 0 || win > 256)
+    return set_error(SEGTACO_EINVAL, "band window of %d rows (32 + 2*halo) > 256", win);
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return set_error(SEGTACO_EUNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
+  CUtensorMap tm;
+  const cuuint64_t dims[2] = {(cuuint64_t)L.N, (cuuint64_t)L.K};
+  const cuuint64_t strides[1] = {(cuuint64_t)L.ldb * sizeof(BT)};
+  const cuuint32_t box[2] = {(cuuint32_t)kBandCols, (cuuint32_t)win};
+  const cuuint32_t es[2] = {1, 1};
+  const CUresult r = enc(&tm, sizeof(BT) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                               : CU_TENSOR_MAP_DATA_TYPE_UINT16,
+                         2, const_cast<void *>(L.B), dims, strides, box, es,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    return set_error(SEGTACO_EINVAL, "band: tensor map of B rejected (CUresult %d)", (int)r);
+  const size_t bytes = band_smem<BT>(win).bytes;
+  auto kern = spmm_band_kernel<BT>;
+  static std::atomic<unsigned long long> opted{0};
+  int dev = 0;
+  SEGTACO_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (!(opted.load() & bit)) {
+    SEGTACO_TRY(check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)(200 * 1024)),
+                           "cudaFuncSetAttribute(spmm_band_kernel)"));
+    opted.fetch_or(bit);
+  }
+  if (bytes > 200 * 1024) return set_error(SEGTACO_EINVAL, "band tiles of %zu bytes > 200 KB", bytes);
+  int *status = nullptr;
+  SEGTACO_TRY(tma_status_ptr(&status));
+  const SpmmArgs<BT> a = make_spmm_args<BT>(L);
+  const dim3 grid((unsigned)((L.M + kBandRows - 1) / kBandRows),
+                  (unsigned)((L.N + kBandCols - 1) / kBandCols), 1);
+  kern<<<grid, kSpmmCta, bytes, s>>>(a, tm, L.band_halo, status);
+  return check_launch("spmm_band_kernel");
+}
+
 // Nonzeros within `halo` of the diagonal (row i scaled to column i*K/M).
 __global__ void band_stats_kernel(const int *__restrict__ row_ptr, const int *__restrict__ col,
                                   int M, int K, int halo, unsigned long long *out) {
@@ -221,6 +471,11 @@ bool window_variant_exists(int dtype, int V, int G) {
 
 int launch_spmm_window(const SpmmLaunch &L, cudaStream_t s) {
   return L.dtype == SEGTACO_BF16 ? launch_window<uint16_t>(L, s) : launch_window<float>(L, s);
+}
+
+int launch_spmm_band(const SpmmLaunch &L, cudaStream_t s) {
+  return L.dtype == SEGTACO_BF16 ? launch_band_typed<uint16_t>(L, s)
+                                 : launch_band_typed<float>(L, s);
 }
 
 }  // namespace segtaco

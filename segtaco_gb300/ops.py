@@ -260,9 +260,10 @@ def autotune(A, n: int, b_dtype=N.F32, schedule=N.AUTO, max_row_len: int | None 
     """The library's configuration for C = A @ B with n columns
     (segtaco_autotune_heuristic): the schedule (AUTO: row-balanced for even
     rows, merge path otherwise), slab, lanes, units; for row-balanced
-    schedules with rows of >= 2048 nonzeros from 1M nonzeros on, the long-row
-    CTAs; and, when at least half of the nonzeros lie within 32 columns of the
-    diagonal, the row-block window of B staged by TMA.  `A` is a DeviceCSR
+    schedules from 1M nonzeros on, long rows out of the row blocks (rb_sr:
+    rows of >= 2048 nonzeros to CTAs of their own; rb_pr: rows of >= 512 as
+    pieces); and, when at least half of the nonzeros lie within 32 columns of
+    the diagonal, rb_pr's band kernel (N >= 64, a multiple of 16).  `A` is a DeviceCSR
     (statistics from segtaco_row_stats / segtaco_band_stats on the device) or
     a host CSR (from its arrays), unless max_row_len is given."""
     banded = False

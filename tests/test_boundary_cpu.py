@@ -279,9 +279,11 @@ def test_device_available_is_a_query(native_lib):
 
 
 def test_window_plan(native_lib):
-    """SEGTACO_FLAG_WINDOW plans the TMA-staged row-block kernel only where the
-    tensor copy is legal (B 16-byte aligned, row pitch a multiple of 16 bytes,
-    window of at most 256 rows and 60 KB) and for row-block schedules."""
+    """SEGTACO_FLAG_WINDOW plans rb_pr's band kernel where it applies (N >= 64
+    and a multiple of 16, B and C 16-byte aligned, B's row pitch a multiple of
+    16 bytes, ldc a multiple of 4, 32 + 2H <= 256 window rows), else the
+    TMA-staged row-block kernel where that tensor copy is legal (window of at
+    most 256 rows and 60 KB), and only for row-block schedules."""
     L = native_lib
     buf = C.create_string_buffer(256)
 
@@ -293,22 +295,31 @@ def test_window_plan(native_lib):
                                           rows_per_unit=k.get("rpu", 16),
                                           items_per_unit=k.get("halo", 32),
                                           col_tile=k.get("tile", 64), vec=k.get("vec", 8))
-    assert " window V=8 G=8 " in plan(64, N.F32, 64, mk(N.RB_PR))
-    assert " window V=2 G=32 " in plan(64, N.F32, 64, mk(N.RB_SR, vec=0))
-    assert " window V=16 G=4 " in plan(64, N.BF16, 64, mk(N.RB_PR, vec=16))
-    assert " window " not in plan(64, N.F32, 64, mk(N.EB_PR))          # rb only
-    assert " window " not in plan(64, N.F32, 66, mk(N.RB_PR, vec=2))   # pitch 264 B
-    assert " window " not in plan(64, N.F32, 64, mk(N.RB_PR), B=0x10000008)  # 8-byte aligned
-    assert " window " not in plan(64, N.F32, 64, mk(N.RB_PR, rpu=32, halo=96))  # 320 rows
-    assert " window " not in plan(64, N.F32, 64, mk(N.RB_PR, rpu=32, halo=64))  # 64 KB
-    # the heuristic takes band statistics but does not choose the window (slower
-    # than plain row blocks on the banded configuration); a B that fits L2 under
-    # a large product gets one 64-column slab of 8-column lanes
-    for flags in (N.FLAG_WINDOW, 0):
+    assert " band " in plan(64, N.F32, 64, mk(N.RB_PR))
+    assert " band " in plan(128, N.BF16, 128, mk(N.RB_PR, vec=16))
+    assert " band " in plan(80, N.F32, 80, mk(N.RB_PR))
+    assert " band " in plan(64, N.F32, 64, mk(N.RB_PR, halo=112))       # 256 window rows
+    assert " band " not in plan(64, N.F32, 64, mk(N.RB_PR, halo=113))   # 258
+    assert " window V=8 G=4 " in plan(48, N.F32, 48, mk(N.RB_PR, tile=48))  # N < 64: window
+    assert " window V=2 G=32 " in plan(64, N.F32, 64, mk(N.RB_SR, vec=0))   # rb_sr: window
+    assert " window V=16 G=4 " in plan(48, N.BF16, 48, mk(N.RB_PR, vec=16))
+    for name in (plan(64, N.F32, 64, mk(N.EB_PR)),                      # rb only
+                 plan(64, N.F32, 66, mk(N.RB_PR, vec=2)),               # pitch 264 B
+                 plan(64, N.F32, 64, mk(N.RB_PR), B=0x10000008)):       # 8-byte aligned
+        assert " window " not in name and " band " not in name, name
+    assert " window " not in plan(48, N.F32, 48, mk(N.RB_PR, rpu=32, halo=96, tile=48))  # 320 rows
+    # the heuristic reads the bit as band statistics: rb_pr keeps it (the band
+    # kernel, halo 32); without it a B that fits L2 under a large product gets
+    # one 64-column slab of 8-column lanes
+    for flags, want in ((N.FLAG_WINDOW, N.FLAG_WINDOW), (0, 0)):
         h = N.Config.make(schedule=N.AUTO, flags=flags)
         assert L.segtaco_autotune_heuristic(262144, 262144, 19135456, 64, N.F32, 73,
                                             C.byref(h)) == N.OK
-        assert (h.schedule, h.flags, h.col_tile, h.vec) == (N.RB_PR, 0, 64, 8)
+        assert (h.schedule, h.flags, h.col_tile, h.vec) == (N.RB_PR, want, 64, 8)
+    h = N.Config.make(schedule=N.RB_SR, flags=N.FLAG_WINDOW)  # rb_sr: not chosen
+    assert L.segtaco_autotune_heuristic(262144, 262144, 19135456, 64, N.F32, 73,
+                                        C.byref(h)) == N.OK
+    assert not h.flags & N.FLAG_WINDOW
     h = N.Config.make(schedule=N.AUTO)  # B of 512 MB: 32-column slabs
     assert L.segtaco_autotune_heuristic(10**6, 10**6, 2 * 10**7, 128, N.F32, 48679,
                                         C.byref(h)) == N.OK

@@ -3,7 +3,10 @@ same products as the row-block kernel, whatever share of the gathers the
 window serves -- banded and scattered matrices, fp32 and bf16 B, slabs cut by
 N, window heights, the top and bottom edges (rows outside B zero-filled by the
 copy), strided and offset B; rb_sr stays bit-exact with the sequential FMA
-order."""
+order.  rb_pr with N >= 64 takes the band kernel (32-row blocks, the band of A
+as a dense tile, off-band nonzeros gathered): the same cases against the FP64
+oracle, halos 0..112, N not a multiple of the 64-column slab, rows past the
+last block, matrices with no band at all."""
 import numpy as np
 import pytest
 import torch
@@ -23,9 +26,14 @@ def _cfg(sched, rpu=16, halo=32, col_tile=0, vec=0, flags=N.FLAG_WINDOW):
     return c
 
 
-def _spmm(Ad, Bd, cfg):
-    """The product through the window kernel (the plan must pick it)."""
-    assert " window " in ops.plan_name(Ad, Bd, cfg), ops.plan_name(Ad, Bd, cfg)
+def _spmm(Ad, Bd, cfg, kernel="window"):
+    """The product through the window kernel, or for rb_pr with N >= 64 (a
+    multiple of 16) and 16-byte aligned operands the band kernel (the plan
+    must pick it)."""
+    name = ops.plan_name(Ad, Bd, cfg)
+    if kernel == "window" and cfg.schedule == N.RB_PR and " band " in name:
+        kernel = "band"
+    assert (" %s " % kernel) in name, name
     return ops.spmm(Ad, Bd, config=cfg)
 
 
@@ -103,8 +111,14 @@ def test_window_overwrites_c(cuda):
     A = SHORT_BAND
     B = synth.dense(A.K, 64, seed=52)
     Cd = torch.full((A.M, 64), float("nan"), device="cuda")
-    Ad, Bd, c = dev(A), torch.from_numpy(B).cuda(), _cfg(N.RB_PR, col_tile=64, vec=8)
-    assert " window " in ops.plan_name(Ad, Bd, c)
+    Ad, Bd = dev(A), torch.from_numpy(B).cuda()
+    for c, kernel in ((_cfg(N.RB_PR, col_tile=64, vec=8), " band "),
+                      (_cfg(N.RB_SR, col_tile=64), " window ")):
+        assert kernel in ops.plan_name(Ad, Bd, c)
+        Cd.fill_(float("nan"))
+        ops.spmm(Ad, Bd, C_out=Cd, config=c)
+        torch.cuda.synchronize()
+        assert_spmm_close(Cd.cpu().numpy(), A, B)
     ops.spmm(Ad, Bd, C_out=Cd, config=c)
     torch.cuda.synchronize()
     assert_spmm_close(Cd.cpu().numpy(), A, B)
@@ -117,11 +131,65 @@ def test_band_stats_and_autotune(cuda):
     assert 2 * k >= BANDED.nnz
     P = synth.power_law(5000, 4000, 1.8, 1500, 0.02, seed=47)
     assert 10 * ops.band_stats(dev(P), 32) < P.nnz
-    # the autotuner measures the band but keeps the plain row blocks (faster on
-    # GB300); the window stays an explicit request
-    assert not ops.autotune(Ad, 64).flags & N.FLAG_WINDOW
-    c = _cfg(N.RB_PR, col_tile=64, vec=8)
+    # the autotuner measures the band and takes the band kernel for rb_pr
+    # (N >= 64); the window for the row-block walk stays an explicit request
+    c = ops.autotune(Ad, 64)
+    assert c.schedule == N.RB_PR and c.flags & N.FLAG_WINDOW and c.items_per_unit == 32
     B = synth.dense(BANDED.K, 64, seed=53)
-    C = _spmm(Ad, torch.from_numpy(B).cuda(), c)
+    C = _spmm(Ad, torch.from_numpy(B).cuda(), c, kernel="band")
     torch.cuda.synchronize()
     assert_spmm_close(C.cpu().numpy(), BANDED, B)
+    assert not ops.autotune(Ad, 32).flags & N.FLAG_WINDOW  # N < 64: plain row blocks
+    assert not ops.autotune(dev(P), 64).flags & N.FLAG_WINDOW  # no band
+
+
+@pytest.mark.parametrize("n", [64, 128, 80, 96, 256])
+@pytest.mark.parametrize("name", ["banded", "short_band", "powerlaw", "rect", "half_empty"])
+def test_band_kernel(cuda, name, n):
+    A = {"banded": BANDED, "short_band": SHORT_BAND,
+         "powerlaw": synth.power_law(5000, 4000, 1.8, 1500, 0.02, seed=47),
+         "rect": synth.random_csr(2000, 700, 0.03, seed=48),
+         "half_empty": synth.random_csr(1500, 3100, 0.01, seed=49, p_empty=0.5)}[name]
+    B = synth.dense(A.K, n, seed=54 + n)
+    Cd = torch.full((A.M, n), float("nan"), device="cuda")
+    Ad, Bd = dev(A), torch.from_numpy(B).cuda()
+    c = N.Config.make(schedule=N.RB_PR, flags=N.FLAG_WINDOW)
+    assert " band " in ops.plan_name(Ad, Bd, c), ops.plan_name(Ad, Bd, c)
+    ops.spmm(Ad, Bd, C_out=Cd, config=c)
+    torch.cuda.synchronize()
+    assert_spmm_close(Cd.cpu().numpy(), A, B)
+
+
+@pytest.mark.parametrize("halo", [0, 1, 8, 32, 64, 112])
+def test_band_halos(cuda, halo):
+    B = synth.dense(BANDED.K, 64, seed=55)
+    c = N.Config.make(schedule=N.RB_PR, items_per_unit=halo, flags=N.FLAG_WINDOW)
+    if halo == 0:
+        c.items_per_unit = 0  # 0 = the default halo of 32
+    C = _spmm(dev(BANDED), torch.from_numpy(B).cuda(), c, kernel="band")
+    torch.cuda.synchronize()
+    assert_spmm_close(C.cpu().numpy(), BANDED, B)
+
+
+@pytest.mark.parametrize("n", [64, 128])
+def test_band_bf16_strided_and_edges(cuda, n):
+    """bf16 B; B a strided view 16 bytes into its allocation; 3,001 rows (a
+    last block of one row); values all one (vals = NULL)."""
+    A = synth.banded_plus_random(3001, 16, 4, seed=56)
+    bits = synth.to_bf16_bits(synth.dense(A.K, n, seed=57))
+    C = _spmm(dev(A), to_torch_bf16(bits), N.Config.make(schedule=N.RB_PR, flags=N.FLAG_WINDOW),
+              kernel="band")
+    torch.cuda.synchronize()
+    assert_spmm_close(C.cpu().numpy(), A, bits, bf16=True)
+    big = torch.from_numpy(synth.dense(A.K, n + 16, seed=58)).cuda()
+    Bv = big[:, 4:4 + n]
+    C = _spmm(dev(A), Bv, N.Config.make(schedule=N.RB_PR, flags=N.FLAG_WINDOW), kernel="band")
+    torch.cuda.synchronize()
+    assert_spmm_close(C.cpu().numpy(), A, Bv.cpu().numpy())
+    ones = synth.CSR(A.row_ptr, A.col, np.ones_like(A.val), A.M, A.K)
+    Ad = ops.DeviceCSR.from_host(ones, "cuda", with_values=False)
+    B = synth.dense(A.K, n, seed=59)
+    C = _spmm(Ad, torch.from_numpy(B).cuda(), N.Config.make(schedule=N.RB_PR, flags=N.FLAG_WINDOW),
+              kernel="band")
+    torch.cuda.synchronize()
+    assert_spmm_close(C.cpu().numpy(), ones, B)
