@@ -203,7 +203,8 @@ __global__ void __launch_bounds__(kSpmmCta)
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  for (int e = t; e < win * kBandPitch; e += kSpmmCta) at[e] = 0.0f;
+  for (int e = t; e < win * kBandPitch / 4; e += kSpmmCta)
+    reinterpret_cast<float4 *>(at)[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   if (t <= kBandRows) rp[t] = __ldg(a.row_ptr + min(i0 + t, M));
   if (t < kBandRows) cnt[t] = 0;
   __syncthreads();
@@ -219,20 +220,21 @@ __global__ void __launch_bounds__(kSpmmCta)
         "l"(&tm), "r"((int)(blockIdx.y * kBandCols)), "r"(jw0), "r"(b)
         : "memory");
   }
-  // Scatter the block's nonzeros rp[0] .. rp[32]-1, four per thread per pass
+  // Scatter the block's nonzeros rp[0] .. rp[32]-1, eight per thread per pass
   // (loads first, then the row searches and shared-memory updates).
+  constexpr int SQ = 8;
   const int k_end = rp[kBandRows];
-  for (int k0 = rp[0] + t; k0 < k_end; k0 += 4 * kSpmmCta) {
-    int cj[4];
-    float cv[4];
+  for (int k0 = rp[0] + t; k0 < k_end; k0 += SQ * kSpmmCta) {
+    int cj[SQ];
+    float cv[SQ];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < SQ; ++q) {
       const int k = k0 + q * kSpmmCta;
       cj[q] = k < k_end ? __ldg(a.col + k) : 0;
       cv[q] = k < k_end ? ld_val(a.val, k) : 0.0f;
     }
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < SQ; ++q) {
       const int k = k0 + q * kSpmmCta;
       if (k < k_end) {
         int r = 0;  // the last row whose start is <= k
@@ -264,6 +266,17 @@ __global__ void __launch_bounds__(kSpmmCta)
   float acc[4][4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.0f;
+  // The first off-band gathers of row 4rb, issued before the tile product so
+  // that their latency hides behind it.
+  const int n0 = cnt[4 * rb];
+  const int pre = n0 <= kBandList ? min(n0, 8) : 0;
+  float4 g0[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    // slots past the row's list gather B row 0 (in bounds) and are not used
+    const int j = e < pre ? lcol[4 * rb * kBandList + e] : 0;
+    g0[e] = band_b4_global<BT>(a.B + (size_t)(unsigned)j * a.ldb + c0);
+  }
   const float *acol = at + 4 * rb;
   const BT *bcol = bw + 4 * cb;
 #pragma unroll 4
@@ -277,11 +290,14 @@ __global__ void __launch_bounds__(kSpmmCta)
   }
   // Off-band nonzeros of the thread's four rows, from global memory.
 #pragma unroll
+  for (int e = 0; e < 8; ++e)
+    if (e < pre) band_fma4(acc[0], lval[4 * rb * kBandList + e], g0[e]);
+#pragma unroll
   for (int q = 0; q < 4; ++q) {
     const int r = 4 * rb + q;
     const int n = cnt[r];
     if (n <= kBandList) {
-      for (int e0 = 0; e0 < n; e0 += 8) {
+      for (int e0 = q == 0 ? pre : 0; e0 < n; e0 += 8) {
         float4 g[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
