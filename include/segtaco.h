@@ -432,8 +432,13 @@ int segtaco_sddmm(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr, con
 #define SEGTACO_SDDMM_AUTO 0
 #define SEGTACO_SDDMM_FIXED 1
 #define SEGTACO_SDDMM_GENERAL 2
+#define SEGTACO_SDDMM_BAND 3 /* rows near the diagonal: 32-row blocks, the dense tile of
+                                their dot products with the Y window of 96 rows around
+                                the diagonal, off-band nonzeros from global memory;
+                                D = 64, ldx and ldy multiples of 4, X and Y aligned to
+                                4 elements (otherwise ignored) */
 typedef struct segtaco_sddmm_config {
-  int32_t kernel;     /* SEGTACO_SDDMM_AUTO / _FIXED / _GENERAL                     */
+  int32_t kernel;     /* SEGTACO_SDDMM_AUTO / _FIXED / _GENERAL / _BAND             */
   int32_t block_nnz;  /* nonzeros per warp block, a power of two 32 .. 4096 (0: 256) */
   int32_t lanes;      /* lanes per dot product (0: from D; power of two); a count
                          the fixed kernel has no shape for (one 32-byte load per
@@ -442,10 +447,12 @@ typedef struct segtaco_sddmm_config {
   int32_t reserved;
 } segtaco_sddmm_config;
 /* The library's SDDMM configuration for this shape: the block size so that a
- * small problem still fills the GPU (at least two waves of warps), the lanes
- * per dot product from D, the element type and the row lengths (rows of a
- * few nonzeros reuse X[i] little, so fewer lanes with more loads each).
- * max_row_len < 0 if unknown. */
+ * small problem still fills the GPU (at least two waves of warps); the kernel
+ * family and the lanes per dot product follow from D, the element type and
+ * the operands' alignment at launch.  cfg->kernel == SEGTACO_SDDMM_BAND on
+ * entry reports that the nonzeros lie near the diagonal (segtaco_band_stats):
+ * it is kept for fp32 factors with D = 64.  max_row_len (< 0 if unknown) is
+ * accepted and not used. */
 int segtaco_sddmm_autotune(int32_t M, int32_t K, int64_t nnz, int32_t D, int32_t x_dtype,
                            int64_t max_row_len, segtaco_sddmm_config *cfg);
 /* segtaco_sddmm with an explicit configuration (NULL: segtaco_sddmm_autotune

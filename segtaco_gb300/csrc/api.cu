@@ -634,8 +634,15 @@ int segtaco_sddmm_autotune(int32_t M, int32_t K, int64_t nnz, int32_t D, int32_t
                            int64_t max_row_len, segtaco_sddmm_config *cfg) {
   if (!cfg) return set_error(SEGTACO_EINVAL, "cfg is NULL");
   if (M < 0 || K < 0 || nnz < 0 || D < 0) return set_error(SEGTACO_EINVAL, "negative size");
+  const bool banded = cfg->kernel == SEGTACO_SDDMM_BAND;
   memset(cfg, 0, sizeof(*cfg));
   cfg->kernel = SEGTACO_SDDMM_AUTO;
+  // Rows known to lie near the diagonal: the band kernel (sddmm_band.cu) for
+  // fp32 factors.  Measured on GB300, banded-plus-random 262,144 rows, D = 64:
+  // fp32 0.334 -> 0.301 ms; bf16 factors stay with the warp-block kernel
+  // (0.304 ms against 0.337: it gathers half the bytes per Y row, while the
+  // band kernel's tiles are fp32 either way).
+  if (banded && D == 64 && x_dtype == SEGTACO_F32) cfg->kernel = SEGTACO_SDDMM_BAND;
   // Blocks of 256 nonzeros per warp; smaller for small problems, so that the
   // launch still holds two waves of warps (152 SMs x 32 warps).
   const long long two_waves = 2LL * 152 * 32;
@@ -644,7 +651,6 @@ int segtaco_sddmm_autotune(int32_t M, int32_t K, int64_t nnz, int32_t D, int32_t
   cfg->block_nnz = blk;
   cfg->lanes = 0;  // from D (sddmm_shape)
   (void)max_row_len;
-  (void)x_dtype;
   (void)K;
   return SEGTACO_OK;
 }
@@ -669,9 +675,12 @@ int segtaco_sddmm_ex(int32_t M, int32_t K, int64_t nnz, const int32_t *row_ptr,
     return set_error(SEGTACO_EINVAL, "block_nnz=%lld not a power of two in [32, 4096]", P);
   if (c.lanes < 0 || c.lanes > 32 || (c.lanes & (c.lanes - 1)))
     return set_error(SEGTACO_EINVAL, "lanes=%d not 0 or a power of two up to 32", c.lanes);
-  if (c.kernel < SEGTACO_SDDMM_AUTO || c.kernel > SEGTACO_SDDMM_GENERAL)
+  if (c.kernel < SEGTACO_SDDMM_AUTO || c.kernel > SEGTACO_SDDMM_BAND)
     return set_error(SEGTACO_EINVAL, "unknown SDDMM kernel %d", c.kernel);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (c.kernel == SEGTACO_SDDMM_BAND && sddmm_band_applies(x_dtype, D, ldx, ldy, X, Y))
+    return launch_sddmm_band(M, K, nnz, row_ptr, col, vals, X, Y, x_dtype, ldx, ldy, D, out, s);
+  if (c.kernel == SEGTACO_SDDMM_BAND) c.kernel = SEGTACO_SDDMM_AUTO;
   const long long nblk = (nnz + P - 1) / P;
   Scratch scratch(nullptr, 0, s);
   SEGTACO_TRY(scratch.reserve(align256((size_t)(nblk + 1) * sizeof(int))));

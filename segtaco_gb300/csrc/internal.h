@@ -171,6 +171,14 @@ int launch_sddmm_multi(const SddmmShape &sh, int x_dtype, const SddmmProblem *pr
                        long long total_blocks, cudaStream_t s);
 // `starts_ready`: `starts` already holds the block starts of this row_ptr (a
 // cached matrix), so only the product is launched.
+// SDDMM of a banded matrix (sddmm_band.cu): 32-row blocks, the dense tile of
+// X-block x Y-window dot products, off-band nonzeros from global memory.  D =
+// 64, ldx and ldy multiples of 4, X and Y aligned to 4 elements.
+bool sddmm_band_applies(int x_dtype, int D, long long ldx, long long ldy, const void *X,
+                        const void *Y);
+int launch_sddmm_band(int M, int K, long long nnz, const int *row_ptr, const int *col,
+                      const float *val, const void *X, const void *Y, int x_dtype, long long ldx,
+                      long long ldy, int D, float *out, cudaStream_t s);
 int launch_sddmm(int M, long long nnz, const int *row_ptr, const int *col, const float *val,
                  const void *X, const void *Y, int x_dtype, long long ldx, long long ldy, int D,
                  float *out, int *starts, int P, long long nblk, cudaStream_t s,

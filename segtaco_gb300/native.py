@@ -78,7 +78,7 @@ class SddmmConfig(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
-SDDMM_AUTO, SDDMM_FIXED, SDDMM_GENERAL = 0, 1, 2
+SDDMM_AUTO, SDDMM_FIXED, SDDMM_GENERAL, SDDMM_BAND = 0, 1, 2, 3
 
 
 class SpmmProblem(C.Structure):

@@ -151,13 +151,18 @@ def sddmm(A: DeviceCSR, X: torch.Tensor, Y: torch.Tensor, out: torch.Tensor | No
 
 def sddmm_autotune(A, D: int, x_dtype=N.F32, max_row_len: int | None = None):
     """The library's SDDMM configuration (segtaco_sddmm_autotune) for A (a
-    DeviceCSR: longest row from the device; or a host CSR)."""
-    if max_row_len is None:
-        if isinstance(A, DeviceCSR):
+    DeviceCSR: longest row and band statistics from the device; or a host
+    CSR): the band kernel when at least half of the nonzeros lie within 32
+    columns of the diagonal (fp32 factors, D = 64)."""
+    if isinstance(A, DeviceCSR):
+        if max_row_len is None:
             max_row_len = int(row_stats(A)[0])
-        else:
+        banded = A.nnz > 0 and band_stats(A) * 2 >= A.nnz
+    else:
+        if max_row_len is None:
             max_row_len = int(np.diff(A.row_ptr).max()) if A.M > 0 else 0
-    cfg = N.SddmmConfig.make()
+        banded = A.nnz > 0 and in_band_fraction_host(A) >= 0.5
+    cfg = N.SddmmConfig.make(N.SDDMM_BAND if banded else N.SDDMM_AUTO)
     N.check(N.lib().segtaco_sddmm_autotune(A.M, A.K, A.nnz, D, x_dtype, max_row_len,
                                            C.byref(cfg)))
     return cfg

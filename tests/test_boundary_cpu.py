@@ -271,6 +271,27 @@ def test_flag_constants_match_the_header():
     assert len(flags) >= 7
     for name, value in flags.items():
         assert getattr(N, name) == int(value), name
+    kernels = dict(re.findall(r"#define SEGTACO_(SDDMM_[A-Z]+)\s+(\d+)", text))
+    assert set(kernels) == {"SDDMM_AUTO", "SDDMM_FIXED", "SDDMM_GENERAL", "SDDMM_BAND"}
+    for name, value in kernels.items():
+        assert getattr(N, name) == int(value), name
+
+
+def test_sddmm_autotune_band(native_lib):
+    """segtaco_sddmm_autotune keeps SEGTACO_SDDMM_BAND (rows near the diagonal)
+    for fp32 factors with D = 64 only; the Python autotuner sets it from the
+    band statistics."""
+    from segtaco_gb300 import ops, synth
+    for D, dt, want in ((64, N.F32, N.SDDMM_BAND), (32, N.F32, N.SDDMM_AUTO),
+                        (128, N.F32, N.SDDMM_AUTO), (64, N.BF16, N.SDDMM_AUTO)):
+        c = N.SddmmConfig.make(N.SDDMM_BAND)
+        assert native_lib.segtaco_sddmm_autotune(262144, 262144, 19135456, D, dt, 73,
+                                                 C.byref(c)) == N.OK
+        assert c.kernel == want and c.block_nnz == 256
+    assert ops.sddmm_autotune(synth.banded_plus_random(2000, 32, 8, seed=3), 64).kernel == \
+        N.SDDMM_BAND
+    assert ops.sddmm_autotune(synth.random_csr(2000, 2000, 0.01, seed=4), 64).kernel == \
+        N.SDDMM_AUTO
 
 
 def test_device_available_is_a_query(native_lib):
