@@ -1041,10 +1041,9 @@ def run_ours(args, world, rank, local):
     max_len = int(A.row_lengths().max())
 
     def tuned(schedule):
-        """The library's choice for this shape (schedule -1 = let it pick)."""
-        h = N_.Config.make(schedule=schedule)
-        N_.check(N_.lib().segtaco_autotune_heuristic(A.M, A.K, A.nnz, N, N_.F32, max_len, h))
-        return h
+        """The library's choice for this shape (schedule -1 = let it pick), from
+        the row and band statistics of the matrix on the device."""
+        return ops.autotune(Ad, N, N_.F32, schedule=schedule, max_row_len=max_len)
 
     cfg = tuned(N_.AUTO if args.schedule == "auto" else N_.SCHEDULES[args.schedule])
     if args.col_tile:
