@@ -146,3 +146,28 @@ def test_sddmm_band_autotuned_full_size(cuda):
         bound = np.abs(A.val[s0:s1]).astype(np.float64) * (
             np.abs(Y32[A.col[s0:s1]]).astype(np.float64) @ np.abs(X32[r]).astype(np.float64))
         assert np.all(np.abs(got[s0:s1] - ref) <= TOL * bound + 1e-30)
+
+
+@pytest.mark.parametrize("m,k", [(1, 1), (1, 300), (31, 31), (33, 40), (97, 5), (5, 3000)])
+def test_sddmm_band_small_shapes(cuda, m, k):
+    """Tiny and ragged shapes through the band SDDMM: one row, one column, a
+    last block of one row, K smaller than the window, wide rectangles."""
+    A = synth.random_csr(m, k, min(1.0, 12.0 / k), seed=m * 11 + k)
+    _check(A, 64, N.F32, N.SddmmConfig.make(N.SDDMM_BAND))
+
+
+def test_sddmm_band_duplicates_and_long_off_band(cuda):
+    """Duplicate entries (each its own output) and blocks with more off-band
+    nonzeros than the 512-entry list (the rest computed per thread)."""
+    rng = np.random.default_rng(78)
+    A = synth.random_csr(3000, 3000, 0.02, seed=79)  # ~60 off-band nonzeros per row
+    rp, cols, vals = [0], [], []
+    for r in range(A.M):
+        s0, s1 = int(A.row_ptr[r]), int(A.row_ptr[r + 1])
+        c = list(A.col[s0:s1]) + list(A.col[s0:s1:9])
+        cols += c
+        vals += list(rng.uniform(-1, 1, len(c)).astype(np.float32))
+        rp.append(len(cols))
+    D = synth.CSR(np.array(rp, np.int32), np.array(cols, np.int32), np.array(vals, np.float32),
+                  A.M, A.K)
+    _check(D, 64, N.F32, N.SddmmConfig.make(N.SDDMM_BAND))

@@ -193,3 +193,71 @@ def test_band_bf16_strided_and_edges(cuda, n):
               kernel="band")
     torch.cuda.synchronize()
     assert_spmm_close(C.cpu().numpy(), ones, B)
+
+
+def _dup_csr(A, seed):
+    """A with every 7th nonzero of each row repeated once (duplicate entries
+    that must add up)."""
+    rng = np.random.default_rng(seed)
+    rows, cols, vals = [], [], []
+    for r in range(A.M):
+        s0, s1 = int(A.row_ptr[r]), int(A.row_ptr[r + 1])
+        c = list(A.col[s0:s1])
+        v = list(A.val[s0:s1])
+        for k in range(0, s1 - s0, 7):
+            c.append(A.col[s0 + k])
+            v.append(np.float32(rng.uniform(-1, 1)))
+        rows.append(len(c))
+        cols += c
+        vals += v
+    rp = np.zeros(A.M + 1, np.int64)
+    np.cumsum(rows, out=rp[1:])
+    return synth.CSR(rp.astype(np.int32), np.array(cols, np.int32), np.array(vals, np.float32),
+                     A.M, A.K)
+
+
+@pytest.mark.parametrize("m,k,n", [(1, 1, 64), (1, 200, 64), (31, 31, 64), (33, 40, 80),
+                                   (40, 40, 64), (97, 5, 64), (5, 3000, 128), (700, 90, 64)])
+def test_band_kernel_small_shapes(cuda, m, k, n):
+    """Tiny and ragged shapes: one row, one column, a last block of 1 row, K
+    smaller than the 96-row window (the copy's rows past K zero-filled), tall
+    and wide rectangles."""
+    A = synth.random_csr(m, k, min(1.0, 12.0 / k), seed=m * 7 + k)
+    B = synth.dense(k, n, seed=m + k)
+    Ad, Bd = dev(A), torch.from_numpy(B).cuda()
+    c = N.Config.make(schedule=N.RB_PR, flags=N.FLAG_WINDOW)
+    assert " band " in ops.plan_name(Ad, Bd, c)
+    Cd = torch.full((m, n), float("nan"), device="cuda")
+    ops.spmm(Ad, Bd, C_out=Cd, config=c)
+    torch.cuda.synchronize()
+    assert_spmm_close(Cd.cpu().numpy(), A, B)
+
+
+def test_band_kernel_duplicate_entries(cuda):
+    """Duplicate (row, column) entries add up in the band tile and in the
+    off-band lists."""
+    A = _dup_csr(synth.banded_plus_random(600, 12, 3, seed=73), 74)
+    B = synth.dense(A.K, 64, seed=75)
+    C = _spmm(dev(A), torch.from_numpy(B).cuda(),
+              N.Config.make(schedule=N.RB_PR, flags=N.FLAG_WINDOW), kernel="band")
+    torch.cuda.synchronize()
+    assert_spmm_close(C.cpu().numpy(), A, B)
+
+
+def test_band_kernel_long_off_band_rows(cuda):
+    """Rows with more off-band nonzeros than the per-row list holds (16) walk
+    their nonzeros in global memory instead."""
+    rng = np.random.default_rng(76)
+    M = K = 2000
+    keys = []
+    for r in range(M):
+        n_off = 40 if r % 5 == 0 else 3
+        cs = set(range(max(0, r - 8), min(K, r + 9)))
+        cs |= set(int(x) for x in rng.integers(0, K, n_off))
+        keys.extend(r * K + np.array(sorted(cs), np.int64))
+    A = synth._from_keys(np.array(keys, np.int64), M, K, rng)
+    B = synth.dense(K, 64, seed=77)
+    C = _spmm(dev(A), torch.from_numpy(B).cuda(),
+              N.Config.make(schedule=N.RB_PR, flags=N.FLAG_WINDOW), kernel="band")
+    torch.cuda.synchronize()
+    assert_spmm_close(C.cpu().numpy(), A, B)
