@@ -183,8 +183,18 @@ __global__ void __launch_bounds__(kLongCta)
     const long long item = item_s;
     __syncthreads();  // everyone has read item_s before it is rewritten
     if (item >= items) break;
-    const long long li = item / slabs;
-    const int slab = (int)(item - li * slabs);
+    // Front part (the longest rows) row by row with all their slabs; the
+    // back part slab by slab, so that its CTAs share one slab of B at a time.
+    long long li;
+    int slab;
+    if (item < n_hi * slabs) {
+      li = item / slabs;
+      slab = (int)(item - li * slabs);
+    } else {
+      const long long it = item - n_hi * slabs;  // n_lo > 0 here
+      slab = (int)(it / n_lo);
+      li = n_hi + (it - (long long)slab * n_lo);
+    }
     const int r = __ldg(list + (li < n_hi ? li : cap_hi + (li - n_hi)));
     const int pb = __ldg(a.row_ptr + r), pe = __ldg(a.row_ptr + r + 1);
     const int col0 = slab * W;
@@ -340,8 +350,10 @@ int launch_long_typed(const SpmmLaunch &L, const int *list, int *counters, int s
   // Slabs of 128 columns (one per row at N <= 128); 32 or 64 for narrower N.
   // rb_sr plans one slot of 32 lanes (G = 32), rb_pr several.
   if (L.G == 32) {
-    if (L.N <= 32) return launch_long_kernel<BT, 32, false>(a, list, counters, sms, s);
-    if (L.N <= 64) return launch_long_kernel<BT, 64, false>(a, list, counters, sms, s);
+    // The row-block kernel's slab width (its B working set) where narrower.
+    const int W = L.V * L.G;
+    if (L.N <= 32 || W <= 32) return launch_long_kernel<BT, 32, false>(a, list, counters, sms, s);
+    if (L.N <= 64 || W <= 64) return launch_long_kernel<BT, 64, false>(a, list, counters, sms, s);
     return launch_long_kernel<BT, 128, false>(a, list, counters, sms, s);
   }
   if (L.N <= 32) return launch_long_kernel<BT, 32, true>(a, list, counters, sms, s);

@@ -46,7 +46,11 @@ def items(front, back, hi_cap, slabs):
         lst[hi_cap + i] = r
     out = []
     for item in range((n_hi + n_lo) * slabs):
-        li, slab = divmod(item, slabs)
+        if item < n_hi * slabs:  # front part: row by row, every slab of a row
+            li, slab = divmod(item, slabs)
+        else:  # back part: slab by slab
+            slab, lo = divmod(item - n_hi * slabs, n_lo)
+            li = n_hi + lo
         idx = li if li < n_hi else hi_cap + (li - n_hi)
         out.append((lst[idx], slab, idx))
     return out

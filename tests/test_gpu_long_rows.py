@@ -209,3 +209,14 @@ def test_rb_pr_pieces_one_and_several(cuda, A, threshold, n):
     got = run(Ad, Bd, n, "rb_pr", **cfg)
     assert_spmm_close(got, A, B)
     assert np.array_equal(got, run(Ad, Bd, n, "rb_pr", **cfg))
+
+
+@pytest.mark.parametrize("col_tile", [64, 32])
+def test_rb_sr_narrow_slabs_bit_identical(cuda, A, col_tile):
+    """rb_sr at 64- and 32-column slabs (N = 128): the long-row CTAs take the
+    row blocks' slab width and the back part of their list slab by slab; every
+    column is still one fmaf chain in storage order."""
+    B = synth.dense(A.K, 128, seed=80)
+    Ad, Bd = dev(A), torch.from_numpy(B).cuda()
+    got = run(Ad, Bd, 128, "rb_sr", col_tile=col_tile)
+    assert np.array_equal(got, rowseq(A, B))

@@ -91,3 +91,6 @@ def test_work_list(seed, T):
         if front and back:
             assert max(i for i, (r, _, _) in enumerate(its) if r in set(front)) < \
                 min(i for i, (r, _, _) in enumerate(its) if r in set(back))
+        # the other rows slab by slab (they share one slab of B at a time)
+        back_slabs = [s for r, s, _ in its if r in set(back)]
+        assert back_slabs == sorted(back_slabs)
