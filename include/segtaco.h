@@ -451,8 +451,8 @@ typedef struct segtaco_sddmm_config {
  * family and the lanes per dot product follow from D, the element type and
  * the operands' alignment at launch.  cfg->kernel == SEGTACO_SDDMM_BAND on
  * entry reports that the nonzeros lie near the diagonal (segtaco_band_stats):
- * it is kept for fp32 factors with D = 64.  max_row_len (< 0 if unknown) is
- * accepted and not used. */
+ * it is kept for D = 64.  max_row_len (< 0 if unknown) is accepted and not
+ * used. */
 int segtaco_sddmm_autotune(int32_t M, int32_t K, int64_t nnz, int32_t D, int32_t x_dtype,
                            int64_t max_row_len, segtaco_sddmm_config *cfg);
 /* segtaco_sddmm with an explicit configuration (NULL: segtaco_sddmm_autotune

@@ -637,12 +637,11 @@ int segtaco_sddmm_autotune(int32_t M, int32_t K, int64_t nnz, int32_t D, int32_t
   const bool banded = cfg->kernel == SEGTACO_SDDMM_BAND;
   memset(cfg, 0, sizeof(*cfg));
   cfg->kernel = SEGTACO_SDDMM_AUTO;
-  // Rows known to lie near the diagonal: the band kernel (sddmm_band.cu) for
-  // fp32 factors.  Measured on GB300, banded-plus-random 262,144 rows, D = 64:
-  // fp32 0.334 -> 0.301 ms; bf16 factors stay with the warp-block kernel
-  // (0.304 ms against 0.337: it gathers half the bytes per Y row, while the
-  // band kernel's tiles are fp32 either way).
-  if (banded && D == 64 && x_dtype == SEGTACO_F32) cfg->kernel = SEGTACO_SDDMM_BAND;
+  // Rows known to lie near the diagonal: the band kernel (sddmm_band.cu).
+  // Measured on GB300, banded-plus-random 262,144 rows, D = 64: fp32 0.330 ->
+  // 0.266 ms, bf16 factors 0.302 -> 0.252 ms.
+  if (banded && D == 64) cfg->kernel = SEGTACO_SDDMM_BAND;
+  (void)x_dtype;
   // Blocks of 256 nonzeros per warp; smaller for small problems, so that the
   // launch still holds two waves of warps (152 SMs x 32 warps).
   const long long two_waves = 2LL * 152 * 32;

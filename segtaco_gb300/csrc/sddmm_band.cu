@@ -142,19 +142,20 @@ __global__ void __launch_bounds__(kSbCta)
     *reinterpret_cast<float4 *>(xr + (e / (kSbD / 4)) * kSbXR + 4 * (e % (kSbD / 4))) = x;
   }
   __syncthreads();
-  // The block's nonzeros, coalesced, four per thread per pass.
+  // The block's nonzeros, coalesced, eight per thread per pass.
+  constexpr int SQ = 8;
   const int k_end = rp[kSbRows];
-  for (int k0 = rp[0] + t; k0 < k_end; k0 += 4 * kSbCta) {
-    int cj[4];
-    float cv[4];
+  for (int k0 = rp[0] + t; k0 < k_end; k0 += SQ * kSbCta) {
+    int cj[SQ];
+    float cv[SQ];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < SQ; ++u) {
       const int k = k0 + u * kSbCta;
       cj[u] = k < k_end ? __ldg(col + k) : 0;
       cv[u] = k < k_end ? (val ? __ldg(val + k) : 1.0f) : 0.0f;
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < SQ; ++u) {
       const int k = k0 + u * kSbCta;
       if (k < k_end) {
         int r = 0;  // the last row whose start is <= k
@@ -189,22 +190,31 @@ __global__ void __launch_bounds__(kSbCta)
   }
   __syncthreads();
   // Listed off-band nonzeros: 16 lanes each (lane l: elements 4l .. 4l+3); a
-  // warp takes two per step and every lane of it takes part in the shuffles.
+  // warp takes two per step, four steps with their gathers in flight at once,
+  // and every lane of it takes part in the shuffles.
   const int n = min(lcount, kSbList);
   const int w = t >> 5, hw = (t >> 4) & 1, l = t & 15;
-  for (int e0 = 2 * w; e0 < n; e0 += kSbCta / 16) {
-    const int e = e0 + hw;
-    const bool ok = e < n;
-    const int4 it = lst[ok ? e : e0];
-    const float4 y = sb_ld4<XT>(Y + (size_t)(unsigned)it.z * ldy + 4 * l);
-    const float4 x = *reinterpret_cast<const float4 *>(xr + it.y * kSbXR + 4 * l);
-    float s = x.x * y.x;
-    s = fmaf(x.y, y.y, s);
-    s = fmaf(x.z, y.z, s);
-    s = fmaf(x.w, y.w, s);
+  constexpr int kSteps = 4, kStride = kSbCta / 16;  // 8 entries per step over the CTA
+  for (int e0 = 2 * w; e0 < n; e0 += kSteps * kStride) {
+    int4 it[kSteps];
+    float4 y[kSteps];
 #pragma unroll
-    for (int o = 8; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, 16);
-    if (ok && l == 0) out[it.x] = __int_as_float(it.w) * s;
+    for (int u = 0; u < kSteps; ++u) {
+      const int e = e0 + u * kStride + hw;
+      it[u] = lst[e < n ? e : e0];  // past the list: entry e0 again, not stored
+      y[u] = sb_ld4<XT>(Y + (size_t)(unsigned)it[u].z * ldy + 4 * l);
+    }
+#pragma unroll
+    for (int u = 0; u < kSteps; ++u) {
+      const float4 x = *reinterpret_cast<const float4 *>(xr + it[u].y * kSbXR + 4 * l);
+      float s = x.x * y[u].x;
+      s = fmaf(x.y, y[u].y, s);
+      s = fmaf(x.z, y[u].z, s);
+      s = fmaf(x.w, y[u].w, s);
+#pragma unroll
+      for (int o = 8; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, 16);
+      if (e0 + u * kStride + hw < n && l == 0) out[it[u].x] = __int_as_float(it[u].w) * s;
+    }
   }
 }
 

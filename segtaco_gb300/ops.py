@@ -153,7 +153,7 @@ def sddmm_autotune(A, D: int, x_dtype=N.F32, max_row_len: int | None = None):
     """The library's SDDMM configuration (segtaco_sddmm_autotune) for A (a
     DeviceCSR: longest row and band statistics from the device; or a host
     CSR): the band kernel when at least half of the nonzeros lie within 32
-    columns of the diagonal (fp32 factors, D = 64)."""
+    columns of the diagonal (D = 64)."""
     if isinstance(A, DeviceCSR):
         if max_row_len is None:
             max_row_len = int(row_stats(A)[0])

@@ -279,11 +279,10 @@ def test_flag_constants_match_the_header():
 
 def test_sddmm_autotune_band(native_lib):
     """segtaco_sddmm_autotune keeps SEGTACO_SDDMM_BAND (rows near the diagonal)
-    for fp32 factors with D = 64 only; the Python autotuner sets it from the
-    band statistics."""
+    for D = 64 only; the Python autotuner sets it from the band statistics."""
     from segtaco_gb300 import ops, synth
     for D, dt, want in ((64, N.F32, N.SDDMM_BAND), (32, N.F32, N.SDDMM_AUTO),
-                        (128, N.F32, N.SDDMM_AUTO), (64, N.BF16, N.SDDMM_AUTO)):
+                        (128, N.F32, N.SDDMM_AUTO), (64, N.BF16, N.SDDMM_BAND)):
         c = N.SddmmConfig.make(N.SDDMM_BAND)
         assert native_lib.segtaco_sddmm_autotune(262144, 262144, 19135456, D, dt, 73,
                                                  C.byref(c)) == N.OK

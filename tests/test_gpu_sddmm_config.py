@@ -132,7 +132,7 @@ def test_sddmm_band_autotuned_full_size(cuda):
     Ad = dev(A)
     cfg = ops.sddmm_autotune(Ad, 64)
     assert cfg.kernel == N.SDDMM_BAND
-    assert ops.sddmm_autotune(Ad, 64, N.BF16).kernel == N.SDDMM_AUTO
+    assert ops.sddmm_autotune(Ad, 64, N.BF16).kernel == N.SDDMM_BAND
     X32, Y32 = synth.dense(A.M, 64, seed=70), synth.dense(A.K, 64, seed=71)
     out = torch.full((A.nnz,), float("nan"), device="cuda")
     ops.sddmm(Ad, torch.from_numpy(X32).cuda(), torch.from_numpy(Y32).cuda(), out, config=cfg)
