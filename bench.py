@@ -1178,16 +1178,21 @@ def run_ours(args, world, rank, local):
         torch.cuda.synchronize()
         n_e2e = max(3, min(args.steps, 10))
         barrier(world)
-        t0 = time.perf_counter()
+        # each drop-in call returns with C on the host: time them one by one
+        # and take the median (one slow call of the host link does not move it)
+        call_s = []
         for _ in range(n_e2e):
+            t0 = time.perf_counter()
             taco.call(name, tC, tA, tB)
-        t_e2e = (time.perf_counter() - t0) / n_e2e
-        t_e2e = reduce_max(t_e2e, world)
+            call_s.append(time.perf_counter() - t0)
+        t_e2e = reduce_max(statistics.median(call_s), world)
+        t_e2e_mean = reduce_max(sum(call_s) / len(call_s), world)
         N_.lib().segtaco_taco_release()
         h2d = (A.M + 1) * 4 + A.nnz * 8 + A.K * N * 4
         e2e = {"value": round(world * byts / t_e2e / 1e9, 3), "unit": UNIT,
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": A.M * N * 4,
-               "ms_per_step": round(t_e2e * 1e3, 3), "entry_point": name}
+               "ms_per_step": round(t_e2e * 1e3, 3), "entry_point": name,
+               "statistic": "median of %d calls (mean %.3f ms)" % (n_e2e, t_e2e_mean * 1e3)}
 
     batched = None
     if not args.no_batched:
