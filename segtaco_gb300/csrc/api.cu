@@ -639,7 +639,7 @@ int segtaco_sddmm_autotune(int32_t M, int32_t K, int64_t nnz, int32_t D, int32_t
   cfg->kernel = SEGTACO_SDDMM_AUTO;
   // Rows known to lie near the diagonal: the band kernel (sddmm_band.cu).
   // Measured on GB300, banded-plus-random 262,144 rows, D = 64: fp32 0.330 ->
-  // 0.266 ms, bf16 factors 0.302 -> 0.252 ms.
+  // 0.245 ms, bf16 factors 0.303 -> 0.224 ms.
   if (banded && D == 64) cfg->kernel = SEGTACO_SDDMM_BAND;
   (void)x_dtype;
   // Blocks of 256 nonzeros per warp; smaller for small problems, so that the

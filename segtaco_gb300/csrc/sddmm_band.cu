@@ -47,7 +47,7 @@ template <typename XT> __device__ __forceinline__ float4 sb_ld4(const XT *p) {
 }
 
 template <typename XT>
-__global__ void __launch_bounds__(kSbCta)
+__global__ void __launch_bounds__(kSbCta, 6)  // 34.4 KB of shared memory: six per SM
     sddmm_band_kernel(int M, int K, const int *__restrict__ row_ptr, const int *__restrict__ col,
                       const float *__restrict__ val, const XT *__restrict__ X,
                       const XT *__restrict__ Y, long long ldx, long long ldy,
@@ -55,8 +55,11 @@ __global__ void __launch_bounds__(kSbCta)
   __shared__ __align__(16) float xt[kSbD * kSbXP];  // xt[d][r]
   __shared__ __align__(16) float yt[kSbD * kSbYP];  // yt[d][jr]; later the tile [r][jr]
   __shared__ int rp[kSbRows + 1];
-  __shared__ int4 lst[kSbList];  // off-band nonzeros: (k, row, column, value bits)
   __shared__ int lcount;
+  // Off-band nonzeros (k, row, column, value bits), in the X block's space once
+  // the tile product no longer reads it.
+  static_assert(kSbList * 4 <= kSbD * kSbXP, "the list fits the transposed X block");
+  int4 *lst = reinterpret_cast<int4 *>(xt);
   const int t = threadIdx.x;
   const int i0 = blockIdx.x * kSbRows;
   const int jw0 = (int)((long long)i0 * K / M) - kSbHalo;
@@ -65,12 +68,13 @@ __global__ void __launch_bounds__(kSbCta)
   // stores them.
   static_assert(kSbRows * (kSbD / 4) == 4 * kSbCta && kSbWin * (kSbD / 4) == 12 * kSbCta,
                 "staging shape");
+  constexpr int kSv = 8;  // vectors in flight per thread
 #pragma unroll
-  for (int pass = 0; pass < 4; ++pass) {
-    float4 v[4];
+  for (int pass = 0; pass < 16 / kSv; ++pass) {
+    float4 v[kSv];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int e = t + (pass * 4 + u) * kSbCta;  // 0 .. 511: X, 512 .. 2047: Y
+    for (int u = 0; u < kSv; ++u) {
+      const int e = t + (pass * kSv + u) * kSbCta;  // 0 .. 511: X, 512 .. 2047: Y
       if (e < kSbRows * (kSbD / 4)) {
         const int i = i0 + e / (kSbD / 4);
         v[u] = i < M ? sb_ld4<XT>(X + (size_t)i * ldx + 4 * (e % (kSbD / 4)))
@@ -83,8 +87,8 @@ __global__ void __launch_bounds__(kSbCta)
       }
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int e = t + (pass * 4 + u) * kSbCta;
+    for (int u = 0; u < kSv; ++u) {
+      const int e = t + (pass * kSv + u) * kSbCta;
       float *dst;
       int pitch, col, q;
       if (e < kSbRows * (kSbD / 4)) {
