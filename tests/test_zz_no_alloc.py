@@ -80,3 +80,27 @@ def test_noalloc_rb_sr_long_rows(cuda):
         assert _noalloc(Ad, Bd, Cd, cfg) == N.OK, N.last_error()
         torch.cuda.synchronize()
         assert np.array_equal(Cd.cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("n", [128, 16])
+def test_noalloc_rb_pr_long_rows(cuda, n):
+    """rb_pr's long rows from 1M nonzeros: at N = 128 the pieces' partial rows
+    do not fit the fixed scratch and the long-row CTAs take them; at N = 16
+    they fit and the pieces run.  Within the FP64 bound and identical call
+    after call either way."""
+    A = synth.power_law(60_000, 50_000, 1.8, 40_000, 0.02, seed=35)
+    assert A.nnz >= 1_000_000 and A.row_lengths().max() >= 512
+    B = synth.dense(A.K, n, seed=37)
+    Ad, Bd = dev(A), torch.from_numpy(B).cuda()
+    cfg = N.Config.make(schedule="rb_pr", flags=N.FLAG_LONG_ROWS)
+    ref = spmm_ref(A, B)
+    first = None
+    for _ in range(2):
+        Cd = torch.full((A.M, n), float("nan"), device="cuda")
+        assert _noalloc(Ad, Bd, Cd, cfg) == N.OK, N.last_error()
+        torch.cuda.synchronize()
+        got = Cd.cpu().numpy()
+        assert_spmm_close(got, A, B, ref=ref)
+        if first is None:
+            first = got
+        assert np.array_equal(got, first)
