@@ -78,10 +78,10 @@ extern "C" {
                                       host thread and device; a call captured
                                       into a graph before that runs both
                                       kernels on the call's stream).  rb_pr:
-                                      pieces of 512 nonzeros inside the
+                                      pieces of 4096 nonzeros inside the
                                       row-block launch, no side stream;
                                       segtaco_autotune_heuristic sets it when
-                                      the longest row reaches that length      */
+                                      the longest row reaches 512 nonzeros     */
 
 #define SEGTACO_FLAG_SLOT_WALK 256u /* eb schedules: every slot of a warp walks its
                                       own merge-path chunk (items_per_unit items,

@@ -190,9 +190,9 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
     const int epc = 16 / esz;
     if (schedule == SEGTACO_RB_PR && pieces) {
       // rb_pr: long rows as pieces of kPieceLen nonzeros in the row-block
-      // launch (spmm_long.cu), over the same column slabs; rows from kPieceLen
-      // nonzeros by default.
-      long long T = c.items_per_unit > 0 ? c.items_per_unit : kPieceLen;
+      // launch (spmm_long.cu), over the same column slabs; rows from
+      // kPieceThreshold nonzeros by default.
+      long long T = c.items_per_unit > 0 ? c.items_per_unit : kPieceThreshold;
       if (T > nnz) T = nnz;
       plan->long_row = (int)T;
       plan->piece_len = (int)kPieceLen;
@@ -383,7 +383,7 @@ int segtaco_autotune_heuristic(int32_t M, int32_t K, int64_t nnz, int32_t N, int
   // fp32 2.32 ms (64-column slabs: 2.45), bf16 2.29 ms (256: 2.52).
   const bool long_rows =
       (schedule == SEGTACO_RB_SR || schedule == SEGTACO_RB_PR) && nnz >= kLongRowsMinNnz &&
-      max_row_len >= (schedule == SEGTACO_RB_PR ? kPieceLen : kLongRowDefault);
+      max_row_len >= (schedule == SEGTACO_RB_PR ? kPieceThreshold : kLongRowDefault);
   if (schedule == SEGTACO_RB_SR && long_rows) cfg->col_tile = 128;
   // fp32 with B beyond L2 (32-column slabs): 8 columns per lane (one 32-byte
   // load, 4 lanes per 128-byte segment, 8 slots), so a warp step covers 8 rows
@@ -421,14 +421,17 @@ int segtaco_autotune_heuristic(int32_t M, int32_t K, int64_t nnz, int32_t N, int
   cfg->depth = (schedule == SEGTACO_RB_SR || schedule == SEGTACO_RB_PR) ? 8 : 4;
   cfg->flags = long_rows ? SEGTACO_FLAG_LONG_ROWS : 0;
   // rb_pr's long rows as pieces of the row-block launch (rows of >= 512
-  // nonzeros); the rows left are short, so a warp takes 32 of them to fill its
-  // slots.  Measured on GB300, 1M x 1M power law, N = 128: 1.69 ms with the
-  // long-row CTAs (threshold 2048, 4 rows per warp), 1.58 with pieces, 1.22
-  // with 32 rows per warp (1.20 with 64; 2 rows: 2.01).  Rows of ~73
-  // nonzeros (banded, N = 64) keep 4: 0.251 ms against 0.266 with 16.
+  // nonzeros, pieces of 4096); the rows left are short, so a warp takes 64 of
+  // them to fill its slots (32 while that leaves fewer than 8192 warps).
+  // Measured on GB300, 1M x 1M power law, N = 128: 1.69 ms with the long-row
+  // CTAs (threshold 2048, 4 rows per warp), 1.58 with pieces of 512, 1.22
+  // with 32 rows per warp (2 rows: 2.01); pieces of 4096: 1.119 ms with 32
+  // rows, 1.114 with 64 (the 10M-nonzero Zipf 1.922 matrix 0.697 / 0.689).
+  // Rows of ~73 nonzeros (banded, N = 64) keep 4: 0.251 ms against 0.266
+  // with 16.
   if (schedule == SEGTACO_RB_PR && long_rows) {
-    cfg->items_per_unit = (int)kPieceLen;
-    if (mean < 32.0) cfg->rows_per_unit = 32;
+    cfg->items_per_unit = (int)kPieceThreshold;
+    if (mean < 32.0) cfg->rows_per_unit = M / 64 >= 8192 ? 64 : 32;
   }
   // fp32 B beyond L2 under skewed rows: the gathered B rows evict_last in L2
   // (A and C stream with evict-first loads and stores).  Measured on GB300,

@@ -205,7 +205,12 @@ constexpr long long kLongRowDefault = 2048;
 inline long long long_row_threshold(const segtaco_config &c) {
   return c.items_per_unit > 0 ? c.items_per_unit : kLongRowDefault;
 }
-// rb_pr splits every row of >= T nonzeros into pieces of S nonzeros.  Rows
+// rb_pr splits every row of >= T nonzeros (default kPieceThreshold) into
+// pieces of S = kPieceLen nonzeros.  Measured on GB300, 1M x 1M power law,
+// N = 128, T = 512, 64 short rows per warp: S = 512 1.193 ms, 1024 1.159,
+// 2048 1.129, 4096 1.114, 8192 1.120, 16384 1.367 (too few pieces to spread
+// the longest rows); T = 256 / 1024 at S = 4096: 1.135 / 1.134 ms.  The
+// 10M-nonzero Zipf 1.922 matrix: 0.689 ms at S = 4096, 0.769 at 8192.  Rows
 // of more than S nonzeros (n = ceil(len / S) <= 2 len / S pieces each, at most
 // 2 nnz / S in all) take the front of the piece list, each piece with a
 // partial row and a counter per column slab; rows of T .. S nonzeros (at most
@@ -213,7 +218,8 @@ inline long long long_row_threshold(const segtaco_config &c) {
 // in int32 entries from the start of the first array: the (row, first
 // nonzero) pairs, the counters, the partial rows (`ld` floats each, 256-byte
 // aligned).
-constexpr long long kPieceLen = 512;
+constexpr long long kPieceLen = 4096;
+constexpr long long kPieceThreshold = 512;
 struct PieceLayout {
   long long multi, cap, ld, ctr, part, entries;
 };

@@ -37,10 +37,11 @@
 // in the workspace and the last piece of a row (a counter per row and slab)
 // sums the partial rows in piece order, so the result is the same from run to
 // run.  Measured on GB300 (1M x 1M power law, N = 128): 1.69 ms with the
-// long-row CTAs, 1.58 with pieces at 4 short rows per warp, 1.20 at 32.  The
-// CTAs (each warp summing a quarter of every stage, the four partials folded
-// at the end) remain for the allocation-free entry point, whose fixed scratch
-// cannot hold the partial rows.
+// long-row CTAs, 1.58 with pieces of 512 at 4 short rows per warp, 1.20 at
+// 32, 1.114 with pieces of 4096 at 64.  The CTAs (each warp summing a
+// quarter of every stage, the four partials folded at the end) remain for the
+// allocation-free entry point where its fixed scratch cannot hold the partial
+// rows.
 #include <algorithm>
 #include <atomic>
 

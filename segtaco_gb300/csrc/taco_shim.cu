@@ -412,7 +412,7 @@ int run_spmm(const Entry &e, taco_tensor_t *C, taco_tensor_t *A, taco_tensor_t *
     // own; rb_pr: pieces) when the host CSR has any.
     if ((e.schedule == SEGTACO_RB_SR || e.schedule == SEGTACO_RB_PR) && nnz >= segtaco::kLongRowsMinNnz) {
       const long long T = e.schedule == SEGTACO_RB_PR && cfg.items_per_unit <= 0
-                              ? segtaco::kPieceLen
+                              ? segtaco::kPieceThreshold
                               : segtaco::long_row_threshold(cfg);
       for (int r = 0; r < M; ++r)
         if (rp[r + 1] - rp[r] >= T) {

@@ -267,7 +267,7 @@ def autotune(A, n: int, b_dtype=N.F32, schedule=N.AUTO, max_row_len: int | None 
     rows, merge path otherwise), slab, lanes, units; for row-balanced
     schedules from 1M nonzeros on, long rows out of the row blocks (rb_sr:
     rows of >= 2048 nonzeros to CTAs of their own; rb_pr: rows of >= 512 as
-    pieces); and, when at least half of the nonzeros lie within 32 columns of
+    pieces of 4096); and, when at least half of the nonzeros lie within 32 columns of
     the diagonal, rb_pr's band kernel (N >= 64, a multiple of 16).  `A` is a DeviceCSR
     (statistics from segtaco_row_stats / segtaco_band_stats on the device) or
     a host CSR (from its arrays), unless max_row_len is given."""

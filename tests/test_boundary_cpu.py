@@ -172,11 +172,11 @@ def test_workspace_and_heuristic(native_lib):
     assert ws(128, items_per_unit=512, flags=LR) == want(512)
     assert ws(128) == 0
     assert ws(126, flags=LR) == 0
-    # rb_pr: pieces of 512 nonzeros, at most 2 nnz / 512 + 1 of rows of
+    # rb_pr: pieces of 4096 nonzeros, at most 2 nnz / 4096 + 1 of rows of
     # several pieces (each with a counter per column slab and a partial row)
     # and nnz / T + 1 one-piece rows; W = 32 columns per slab here, 4 slabs
-    multi = 2 * 2 * 10**7 // 512 + 1  # default threshold for rb_pr: 512
-    cap = multi + 2 * 10**7 // 512 + 1
+    multi = 2 * 2 * 10**7 // 4096 + 1
+    cap = multi + 2 * 10**7 // 512 + 1  # default threshold for rb_pr: 512
     part = (2 * cap + 4 * multi + 63) // 64 * 64
     c = N.Config.make(schedule="rb_pr", flags=LR)
     assert L.segtaco_spmm_workspace_size(10**6, 10**6, 2 * 10**7, 128, N.F32, C.byref(c),
@@ -217,15 +217,19 @@ def test_workspace_and_heuristic(native_lib):
                                             C.byref(h)) == N.OK
         assert h.schedule == sched and h.col_tile == tile and h.vec == 0
         assert h.items_per_unit == items and h.flags == flags
-    # rb_pr: long rows (pieces) from 512 nonzeros, then 32 short rows per warp;
-    # rows known short or unknown: none (unknown: not skewed, no L2 hints)
+    # rb_pr: long rows (pieces) from 512 nonzeros, then 64 short rows per warp
+    # (32 while 64 would leave fewer than 8192 warps); rows known short or
+    # unknown: none (unknown: not skewed, no L2 hints)
     H, LR = N.FLAG_L2_HINTS, N.FLAG_LONG_ROWS
-    for max_len, flags, rows, items in ((511, H, 4, 2048), (512, LR | H, 32, 512),
-                                        (48679, LR | H, 32, 512), (-1, 0, 4, 2048)):
+    for m, max_len, flags, rows, items in ((10**6, 511, H, 4, 2048),
+                                           (10**6, 512, LR | H, 64, 512),
+                                           (10**6, 48679, LR | H, 64, 512),
+                                           (10**6, -1, 0, 4, 2048),
+                                           (300_000, 48679, LR | H, 32, 512)):
         h.schedule = N.RB_PR
-        assert L.segtaco_autotune_heuristic(10**6, 10**6, 2 * 10**7, 128, N.F32, max_len,
+        assert L.segtaco_autotune_heuristic(m, 10**6, m * 20, 128, N.F32, max_len,
                                             C.byref(h)) == N.OK
-        assert (h.flags, h.rows_per_unit, h.items_per_unit) == (flags, rows, items), max_len
+        assert (h.flags, h.rows_per_unit, h.items_per_unit) == (flags, rows, items), (m, max_len)
     h.schedule = N.RB_PR  # long rows under a mean of 73 nonzeros per row: 4 rows per warp
     assert L.segtaco_autotune_heuristic(262144, 262144, 19135456, 64, N.F32, 580,
                                         C.byref(h)) == N.OK

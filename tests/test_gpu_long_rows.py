@@ -7,7 +7,7 @@ storage order, so the result must be bit-identical to the one-warp walk
 (spmm_rb_sr.h:187-243): across thresholds, widths (one and several column
 slabs, widths the 16-byte copies cannot take), bf16 B, unit values, offset B,
 the partition-ready split, and graph capture (the allocation-free entry point:
-test_zz_no_alloc.py).  rb_pr: the long rows are pieces of 512 nonzeros in
+test_zz_no_alloc.py).  rb_pr: the long rows are pieces of 4096 nonzeros in
 the row-block launch (over the same column slabs), whose partial rows the
 last piece of each row sums in piece order: within the FP64 bound of 1e-5 and
 bit-identical from run to run."""
@@ -27,14 +27,16 @@ pytestmark = pytest.mark.gpu
 def A():
     """Short rows (~29 nonzeros, 10 % empty) plus rows of exactly 50,000 /
     20,000 / 5,000 / 1,000 / 600 nonzeros, rows of 2047, 2048 and 2049 (the
-    default threshold's edge) and of 16,383 / 16,384 (where rows move to the
-    front of the work list); 1.1M nonzeros."""
+    default threshold's edge), of 4095 / 4096 / 4097 and 8192 / 8193 (rb_pr's
+    piece length and its double) and of 16,383 / 16,384 (where rows move to
+    the front of the work list); 1.1M nonzeros."""
     rng = np.random.default_rng(41)
     M, K = 41_000, 50_000
     lengths = rng.binomial(64, 0.45, M)
     lengths[rng.random(M) < 0.1] = 0
     long_rows = {7: 50_000, 100: 20_000, 2_000: 5_000, 39_999: 600, 15_000: 2_047,
-                 15_001: 2_048, 15_002: 2_049, 0: 1_000, 30_000: 16_383, 30_001: 16_384}
+                 15_001: 2_048, 15_002: 2_049, 0: 1_000, 30_000: 16_383, 30_001: 16_384,
+                 20_000: 4_095, 20_001: 4_096, 20_002: 4_097, 25_000: 8_192, 25_001: 8_193}
     for r in long_rows:
         lengths[r] = 0
     rows = np.repeat(np.arange(M, dtype=np.int64), lengths)
@@ -199,10 +201,12 @@ def test_rb_pr_pieces_partition_ready_and_graph(cuda, A):
         assert np.array_equal(C_.cpu().numpy(), first)
 
 
-@pytest.mark.parametrize("threshold,n", [(1, 64), (300, 40), (513, 128), (1024, 96)])
+@pytest.mark.parametrize("threshold,n", [(1, 64), (300, 40), (513, 128), (1024, 96),
+                                         (4096, 128), (4097, 72)])
 def test_rb_pr_pieces_one_and_several(cuda, A, threshold, n):
-    """Thresholds at and around the piece length (512): rows of one piece
-    (stored directly) beside rows of several, ragged widths; identical reruns."""
+    """Thresholds below, at and above the piece length (4096): rows of one
+    piece (stored directly) beside rows of several, ragged widths; identical
+    reruns."""
     B = synth.dense(A.K, n, seed=63 + n)
     Ad, Bd = dev(A), torch.from_numpy(B).cuda()
     cfg = dict(items_per_unit=threshold)

@@ -82,12 +82,12 @@ def test_noalloc_rb_sr_long_rows(cuda):
         assert np.array_equal(Cd.cpu().numpy(), want)
 
 
-@pytest.mark.parametrize("n", [128, 16])
+@pytest.mark.parametrize("n", [512, 128, 16])
 def test_noalloc_rb_pr_long_rows(cuda, n):
-    """rb_pr's long rows from 1M nonzeros: at N = 128 the pieces' partial rows
-    do not fit the fixed scratch and the long-row CTAs take them; at N = 16
-    they fit and the pieces run.  Within the FP64 bound and identical call
-    after call either way."""
+    """rb_pr's long rows from 1M nonzeros: at N = 512 the pieces' partial rows
+    (16 slabs of 32 columns) do not fit the fixed scratch and the long-row
+    CTAs take them; at N = 128 and 16 they fit and the pieces run.  Within the
+    FP64 bound and identical call after call either way."""
     A = synth.power_law(60_000, 50_000, 1.8, 40_000, 0.02, seed=35)
     assert A.nnz >= 1_000_000 and A.row_lengths().max() >= 512
     B = synth.dense(A.K, n, seed=37)
