@@ -133,6 +133,18 @@ typedef struct segtaco_config {
                              result does not vary from run to run          */
   uint32_t flags;         /* SEGTACO_FLAG_*                                        */
   int32_t depth;          /* row walk: dense loads in flight per lane (0 = 4, 4, 8) */
+  int32_t k_parts;        /* rb_pr pieces: passes over ranges of B's rows, 1 .. 8
+                             (0: one).  With more than one the pieces (of
+                             2048 nonzeros) run in a launch of their own
+                             before the row blocks, pass p taking the
+                             nonzeros of columns [p*Kp, (p+1)*Kp), Kp = K /
+                             k_parts rounded up, so that a pass gathers from
+                             that range of B only; columns sorted within each
+                             row keep a pass inside its range (unsorted rows
+                             stay correct, without that locality); every
+                             (piece, pass) leaves a partial row, summed in
+                             order.  Opt-in: the short rows then no longer
+                             overlap the pieces                            */
 } segtaco_config;
 
 /* Library identity and build checks. */

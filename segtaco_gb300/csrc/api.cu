@@ -170,6 +170,7 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
   plan->workspace = 0;
   plan->long_row = 0;
   plan->piece_len = 0;
+  plan->piece_parts = 1;
   plan->px_entries = plan->py_entries = 0;
   if (schedule == SEGTACO_EB_SR || schedule == SEGTACO_EB_PR) {
     // merge-path items per chunk: one chunk per warp (512, fewer for small
@@ -195,8 +196,14 @@ int plan_spmm(int M, int K, long long nnz, int N, int b_dtype, long long ldb, lo
       long long T = c.items_per_unit > 0 ? c.items_per_unit : kPieceThreshold;
       if (T > nnz) T = nnz;
       plan->long_row = (int)T;
-      plan->piece_len = (int)kPieceLen;
-      plan->px_entries = piece_layout(nnz, T, kPieceLen, plan->slabs, W).entries;
+      // passes over ranges of B's rows (a launch of their own before the row
+      // blocks) on request
+      int parts = c.k_parts > 0 ? c.k_parts : 1;
+      if (parts > kMaxPieceParts) parts = kMaxPieceParts;
+      if (parts > K) parts = K > 0 ? K : 1;
+      plan->piece_parts = parts;
+      plan->piece_len = (int)(parts > 1 ? kPassPieceLen : kPieceLen);
+      plan->px_entries = piece_layout(nnz, T, plan->piece_len, plan->slabs, W, parts).entries;
       plan->py_entries = 4;  // the count
     } else if (N % epc == 0 && ldb % epc == 0 && ((uintptr_t)B % 16) == 0) {
       // Long rows to CTAs of their own (spmm_long.cu): their ring copies
@@ -281,9 +288,9 @@ int run_spmm_planned(const SpmmPlan &plan, int M, int K, long long nnz, const in
         L.long_row = plan.long_row;
         if (!partition_ready)
           SEGTACO_TRY(launch_long_pieces_list(row_ptr, M, nnz, plan.long_row, plan.piece_len,
-                                              plan.slabs, plan.W, px, py, s));
-        const PieceLayout pl =
-            piece_layout(nnz, plan.long_row, plan.piece_len, plan.slabs, plan.W);
+                                              plan.slabs, plan.W, plan.piece_parts, px, py, s));
+        const PieceLayout pl = piece_layout(nnz, plan.long_row, plan.piece_len, plan.slabs,
+                                            plan.W, plan.piece_parts);
         L.piece_len = plan.piece_len;
         L.pieces = px;
         L.piece_count = py;
@@ -292,6 +299,15 @@ int run_spmm_planned(const SpmmPlan &plan, int M, int K, long long nnz, const in
         L.piece_cap = pl.cap;
         L.piece_multi = pl.multi;
         L.piece_ld = pl.ld;
+        L.piece_parts = plan.piece_parts;
+        // count[2..3]: the passes' work counter (the count array is 256-byte aligned)
+        L.piece_queue = reinterpret_cast<unsigned long long *>(py + 2);
+        if (plan.piece_parts > 1) {
+          // the pieces' passes, then the row blocks of the short rows alone
+          SEGTACO_TRY(bf16 ? launch_spmm_pieces_bf16(L, s) : launch_spmm_pieces_f32(L, s));
+          L.piece_len = 0;
+          L.piece_cap = 0;
+        }
         return bf16 ? launch_spmm_bf16_rows(L, s) : launch_spmm_f32_rows(L, s);
       }
       if (plan.long_row > 0) {
@@ -468,10 +484,10 @@ int segtaco_spmm_plan_name(int32_t M, int32_t K, int64_t nnz, int32_t N, int32_t
                        : plan.window_halo >= 0 ? "window"
                        : plan.long_row > 0 ? (plan.piece_len > 0 ? "pieces" : "long_rows")
                        : (plan.schedule >= SEGTACO_EB_SR) ? "chunks" : "rows";
-  snprintf(out, len, "%s %s V=%d G=%d W=%d slabs=%d walk=%d halo=%d rows_per_unit=%lld",
+  snprintf(out, len, "%s %s V=%d G=%d W=%d slabs=%d walk=%d halo=%d rows_per_unit=%lld parts=%d",
            sched[plan.schedule], kernel, plan.V, plan.G, plan.W, plan.slabs, plan.walk,
            plan.band_halo >= 0 ? plan.band_halo : plan.window_halo,
-           (long long)plan.rows_per_unit);
+           (long long)plan.rows_per_unit, plan.piece_len > 0 ? plan.piece_parts : 1);
   return SEGTACO_OK;
 }
 
@@ -531,7 +547,7 @@ int segtaco_spmm_partition(int32_t M, int32_t K, int64_t nnz, const int32_t *row
   int *py = static_cast<int *>(scratch.take(plan.py_entries * sizeof(int)));
   if (plan.long_row > 0 && plan.piece_len > 0)
     return launch_long_pieces_list(row_ptr, M, nnz, plan.long_row, plan.piece_len, plan.slabs,
-                                   plan.W, px, py, s);
+                                   plan.W, plan.piece_parts, px, py, s);
   if (plan.long_row > 0) return launch_long_rows_list(row_ptr, M, nnz, plan.long_row, px, py, s);
   return launch_merge_path(row_ptr, M, nnz, plan.items_per_unit, plan.nchunks, px, py, C, ldc, N,
                            s);

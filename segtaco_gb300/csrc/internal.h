@@ -92,12 +92,20 @@ struct SpmmLaunch {
   long long piece_cap = 0;        // list entries (both parts)
   long long piece_multi = 0;      // entries of the front part (rows of several pieces)
   long long piece_ld = 0;
+  // > 1: the pieces run in a launch of their own before the row blocks, in
+  // piece_parts passes over ranges of B's rows (spmm_pieces_pass)
+  int piece_parts = 1;
+  unsigned long long *piece_queue = nullptr;  // the passes' work counter (8-byte aligned)
 };
 // One launcher per (dense type, unit kind); each switches over (V, G).
 int launch_spmm_f32_rows(const SpmmLaunch &L, cudaStream_t s);
 int launch_spmm_f32_chunks(const SpmmLaunch &L, cudaStream_t s);
 int launch_spmm_bf16_rows(const SpmmLaunch &L, cudaStream_t s);
 int launch_spmm_bf16_chunks(const SpmmLaunch &L, cudaStream_t s);
+// rb_pr's pieces in piece_parts passes (a persistent launch before the row
+// blocks).
+int launch_spmm_pieces_f32(const SpmmLaunch &L, cudaStream_t s);
+int launch_spmm_pieces_bf16(const SpmmLaunch &L, cudaStream_t s);
 // TMA variants: 16-byte lane vectors only (fp32 x 4, bf16 x 8), any G.
 int launch_spmm_tma_f32(const SpmmLaunch &L, bool rows, cudaStream_t s);
 int launch_spmm_tma_bf16(const SpmmLaunch &L, bool rows, cudaStream_t s);
@@ -128,6 +136,8 @@ struct SpmmPlan {
   int window_halo = -1;      // rb: >= 0 stages each row block's B window (spmm_window.cu)
   int band_halo = -1;        // rb_pr: >= 0 banded row blocks with a dense band tile
   int piece_len = 0;         // rb_pr: long rows split into pieces of this many nonzeros
+  int piece_parts = 1;       // rb_pr pieces: passes over ranges of B's rows (> 1: a launch
+                             // of their own before the row blocks)
   long long px_entries;      // int32 entries of the first workspace array (eb: chunk-edge
                              // rows; rb long rows: the list of long rows)
   long long py_entries;      // ... of the second (eb: chunk-edge nonzeros; long rows: counters)
@@ -220,19 +230,40 @@ inline long long long_row_threshold(const segtaco_config &c) {
 // aligned).
 constexpr long long kPieceLen = 4096;
 constexpr long long kPieceThreshold = 512;
+// Pieces of the passes over ranges of B's rows (piece_parts > 1): shorter, so
+// that each (pass, slab) holds enough of them for every warp of the grid
+// (two passes: 512 1.318 ms, 1024 1.147, 2048 1.081, 4096 1.182).
+constexpr long long kPassPieceLen = 2048;
+//
+// With R > 1 passes over ranges of B's rows (spmm_pieces_pass) every piece
+// leaves R partial rows, one per pass, so every row (one-piece rows too) gets
+// counters and R partial rows per piece: counters for all `cap` entries, the
+// partial rows at (entry * R + pass).
 struct PieceLayout {
   long long multi, cap, ld, ctr, part, entries;
 };
-inline PieceLayout piece_layout(long long nnz, long long T, long long S, int slabs, int W) {
+inline PieceLayout piece_layout(long long nnz, long long T, long long S, int slabs, int W,
+                                int parts = 1) {
   PieceLayout p;
   p.multi = 2 * nnz / S + 1;
   p.cap = p.multi + nnz / T + 1;
   p.ld = (long long)slabs * W;
   p.ctr = 2 * p.cap;
-  p.part = (p.ctr + p.multi * slabs + 63) / 64 * 64;
-  p.entries = p.part + p.multi * p.ld;
+  const long long rows = parts > 1 ? p.cap : p.multi;  // entries with counters / partials
+  p.part = (p.ctr + rows * slabs + 63) / 64 * 64;
+  p.entries = p.part + rows * (parts > 1 ? parts : 1) * p.ld;
   return p;
 }
+// Passes over ranges of B's rows for rb_pr's pieces (segtaco_config.k_parts,
+// at most 8; one by default).  Measured on GB300, 1M x 1M power law, N = 128:
+// the long rows alone (4394 rows of >= 512 nonzeros, each range an SpMM of
+// its own) take 0.567 ms in one pass, 0.423 in two, 0.426 in four; but the
+// passes then run apart from the short rows, which in one pass fill the
+// warps the pieces leave idle, and the whole product gains little or loses:
+// rb_pr 1.098-1.118 ms in one pass, in two 1.081 (pieces of 2048), 1.147
+// (1024), 1.182 (4096); the 10M-nonzero Zipf 1.922 matrix 0.683-0.691 ms in
+// one pass, 0.739-0.850 in two.
+constexpr int kMaxPieceParts = 8;
 // The two parts of the long-row list for threshold T: rows of >= 8T nonzeros
 // (at most nnz / 8T of them) and rows of T .. 8T-1 (at most nnz / T).
 inline void long_list_caps(long long nnz, long long T, long long *hi, long long *lo) {
@@ -248,10 +279,12 @@ int launch_long_rows_list(const int *row_ptr, int M, long long nnz, int long_row
 int launch_spmm_long_rows(const SpmmLaunch &L, const int *list, int *counters, cudaStream_t s);
 // rb_pr: lists every row of >= long_row nonzeros as pieces of piece_len
 // nonzeros into `pieces` (piece_layout: the pairs, the counters of each row's
-// first piece cleared here), counting the front and back parts in count[0]
-// and count[1] (cleared here).
+// first piece cleared here; with parts > 1 those of one-piece rows too),
+// counting the front and back parts in count[0] and count[1] (cleared here).
 int launch_long_pieces_list(const int *row_ptr, int M, long long nnz, int long_row, int piece_len,
-                            int slabs, int W, int *pieces, int *count, cudaStream_t s);
+                            int slabs, int W, int parts, int *pieces, int *count, cudaStream_t s);
+// Multiprocessors of the current device (cached per device).
+int device_sms();
 
 int launch_spmspv(int M, int K, const int *col_ptr, const int *row_idx, const float *val, int nx,
                   const int *x_idx, const float *x_vals, float *y, cudaStream_t s);

@@ -69,6 +69,10 @@ template <typename BT> struct SpmmArgs {
   // piece_multi.  A piece of several stores its partial row (piece_ld floats)
   // and counts itself in piece_ctr[first piece of the row * slabs + slab]; the
   // last piece of a row sums the row's partials in piece order into C.
+  // piece_parts > 1: the pieces run in a launch of their own (spmm_pieces_kernel),
+  // pass p over the nonzeros whose columns lie in [p*Kp, (p+1)*Kp) (Kp = K /
+  // piece_parts rounded up) of every piece, so that a pass gathers from that
+  // range of B's rows only; each (piece, pass) leaves a partial row.
   const int2 *__restrict__ pieces;
   const int *__restrict__ piece_count;
   unsigned *piece_ctr;
@@ -77,6 +81,8 @@ template <typename BT> struct SpmmArgs {
   long long piece_multi;
   long long piece_ld;
   int piece_len;
+  int piece_parts;
+  unsigned long long *piece_queue;  // the passes' work counter (cleared before the launch)
 };
 
 template <int V> __device__ __forceinline__ void zero(float (&a)[V]) {
@@ -163,24 +169,26 @@ template <int R> __device__ __forceinline__ void put_c(float *p, const float *a,
 }
 
 // The end of a piece of a long row (rb_pr): its R sums of columns c0 .. c0+R-1
-// (`mine`: this lane holds such columns) become the piece's partial row; the
-// piece of the row that counts itself last sums the row's partials in piece
-// order and stores them in C, so the result does not depend on which piece
-// finishes first.  A row of one piece stores directly.
+// (`mine`: this lane holds such columns) become the piece's partial row (in
+// pass `pass` of piece_parts); the (piece, pass) of the row that counts
+// itself last sums the row's partials in (piece, pass) order and stores them
+// in C, so the result does not depend on which finishes first.  A row of one
+// piece in one pass stores directly.  y0: the piece's first nonzero.
 template <typename BT, int R>
 __device__ __forceinline__ void finish_piece(const SpmmArgs<BT> &a, long long w, int row, int y0,
                                              int slab, int slabs, const float *acc, bool mine,
-                                             int c0, int lane) {
+                                             int c0, int lane, int pass) {
   const int rs = __ldg(a.row_ptr + row), re = __ldg(a.row_ptr + row + 1);
   const int n = (re - rs + a.piece_len - 1) / a.piece_len;
+  const int np = a.piece_parts;
   float *dst = a.C + (long long)row * a.ldc + c0;
-  if (n == 1) {
+  if (n == 1 && np == 1) {
     if (mine) put_c<R>(dst, acc, false);
     return;
   }
   const long long first = w - (y0 - rs) / a.piece_len;
   if (mine) {
-    float *part = a.piece_part + w * a.piece_ld + c0;
+    float *part = a.piece_part + (w * np + pass) * a.piece_ld + c0;
 #pragma unroll
     for (int k = 0; k < R; ++k) __stcg(part + k, acc[k]);
   }
@@ -189,7 +197,7 @@ __device__ __forceinline__ void finish_piece(const SpmmArgs<BT> &a, long long w,
   unsigned seen = 0;
   if (lane == 0) seen = atomicAdd(a.piece_ctr + first * slabs + slab, 1u);
   seen = __shfl_sync(0xffffffffu, seen, 0);
-  if (seen != (unsigned)(n - 1)) return;
+  if (seen != (unsigned)(n * np - 1)) return;
   __threadfence();
   // every piece of the row has counted itself: the counter is free again (a
   // later product may reuse the list)
@@ -198,13 +206,40 @@ __device__ __forceinline__ void finish_piece(const SpmmArgs<BT> &a, long long w,
     float sum[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) sum[k] = 0.0f;
-    for (int q = 0; q < n; ++q) {
-      const float *part = a.piece_part + (first + q) * a.piece_ld + c0;
+    for (long long q = first * np; q < (first + n) * np; ++q) {
+      const float *part = a.piece_part + q * a.piece_ld + c0;
 #pragma unroll
       for (int k = 0; k < R; ++k) sum[k] += __ldcg(part + k);
     }
     put_c<R>(dst, sum, false);
   }
+}
+
+// First position in [lo, hi) whose column is >= target (hi if none), searched
+// by the whole warp: 32 probes per round narrow the range to one probe step.
+// On a row whose columns are not sorted it still returns a position in [lo,
+// hi], so the passes' ranges [b_p, b_p+1) still cover the piece exactly once.
+__device__ __forceinline__ int warp_lower_bound(const int *__restrict__ col, int lo, int hi,
+                                                long long target, int lane) {
+  const unsigned FULL = 0xffffffffu;
+  while (hi - lo > 32) {
+    const long long step = (hi - lo + 31) / 32;
+    const long long p = lo + lane * step;
+    const bool ge = p >= hi || (long long)__ldg(col + p) >= target;
+    const unsigned m = __ballot_sync(FULL, ge);
+    if (m == 0u) {
+      lo += (int)(31 * step + 1);  // every probe below target (p < hi for all lanes)
+      continue;
+    }
+    const int f = __ffs(m) - 1;
+    const long long nhi = lo + f * step;
+    if (f > 0) lo = (int)(lo + (f - 1) * step + 1);
+    hi = nhi < hi ? (int)nhi : hi;
+  }
+  const long long p = (long long)lo + lane;
+  const bool ge = p < hi && (long long)__ldg(col + p) >= target;
+  const unsigned m = __ballot_sync(FULL, ge);
+  return m ? lo + __ffs(m) - 1 : hi;
 }
 
 // Rows [lo, lo + rows) of the current column slab of B staged in shared
@@ -216,9 +251,12 @@ template <typename BT> struct Window {
 
 // Walk one unit (merge-path chunk or row block) `w` over column slab `slab`.
 // The body of every SpMM kernel below (single problem or batched).
+// pass >= 0 (rb_pr pieces in several passes, spmm_pieces_pass): piece `w`
+// restricted to the nonzeros of that pass's range of B's rows.
 template <typename BT, int V, int G, bool ROWS, bool DEEP, bool WIN = false>
 __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long w, int slab,
-                                               int lane, Window<BT> win = Window<BT>()) {
+                                               int lane, Window<BT> win = Window<BT>(),
+                                               int pass = -1) {
   constexpr int P = 32 / G;                 // slots
   // Rows with >= LONG nonzeros are split over the slots (LONG <= 32, so a
   // short row always fits one batch).
@@ -247,18 +285,28 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
   };
 
   int x0, x1, y0, y1;
+  int py0 = 0;  // a piece's first nonzero
   bool head_split = false, tail_open = false;
   if (ROWS) {
     if (w < a.piece_cap) {
-      // A piece of a long row: its nonzeros [y0, y1), added to the row of C
-      // (zeroed by the list pass) like a merge-path chunk inside one row.
+      // A piece of a long row: its nonzeros [y0, y1) walked like a merge-path
+      // chunk inside one row, the sum left to finish_piece.
       if (w < a.piece_multi ? w >= (long long)__ldg(a.piece_count)
                             : w - a.piece_multi >= (long long)__ldg(a.piece_count + 1))
         return;
       const int2 pc = __ldg(a.pieces + w);
       x0 = x1 = pc.x;
-      y0 = pc.y;
+      py0 = y0 = pc.y;
       y1 = min(pc.y + a.piece_len, __ldg(a.row_ptr + pc.x + 1));
+      if (pass >= 0) {
+        // this pass's range [b_pass, b_pass+1) of the piece: b_0 = y0, b_R =
+        // y1, b_p the first nonzero of column >= p*Kp at or after b_p-1
+        const long long Kp = ((long long)a.K + a.piece_parts - 1) / a.piece_parts;
+        int lo = y0;
+        for (int q = 1; q <= pass; ++q) lo = warp_lower_bound(a.col, lo, y1, q * Kp, lane);
+        if (pass + 1 < a.piece_parts) y1 = warp_lower_bound(a.col, lo, y1, (pass + 1) * Kp, lane);
+        y0 = lo;
+      }
       head_split = tail_open = true;
     } else {
       const long long r0 = (w - a.piece_cap) * a.rows_per_unit;
@@ -404,9 +452,10 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
         bool owner;
         const int first = fold_slots_scatter<G, V>(acc, lane, owner);
         if (ROWS && piece) {
-          finish_piece<BT, fold_scatter_count<G, V>()>(a, w, cur, y0, slab,
+          finish_piece<BT, fold_scatter_count<G, V>()>(a, w, cur, py0, slab,
                                                        (a.N + G * V - 1) / (G * V), acc,
-                                                       active && owner, col0 + first, lane);
+                                                       active && owner, col0 + first, lane,
+                                                       pass < 0 ? 0 : pass);
         } else if (active && owner) {
           const bool edge = (cur == x0 && head_split) || (cur == x1 && tail_open);
           constexpr int R = fold_scatter_count<G, V>();
@@ -414,8 +463,8 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
                                             edge);
         }
       } else if (ROWS && piece) {
-        finish_piece<BT, V>(a, w, cur, y0, slab, (a.N + G * V - 1) / (G * V), acc, active, col0,
-                            lane);
+        finish_piece<BT, V>(a, w, cur, py0, slab, (a.N + G * V - 1) / (G * V), acc, active, col0,
+                            lane, pass < 0 ? 0 : pass);
       } else if (active) {
         float *dst = a.C + (long long)cur * a.ldc + col0;
         if ((cur == x0 && head_split) || (cur == x1 && tail_open))
@@ -943,6 +992,110 @@ template <int V, int G, bool HEAVY> constexpr int spmm_min_ctas() {
   // warps without the spill); wider groups, the flat walk with 8-element
   // lanes and the deep row walk take 24 warps.
   return ((HEAVY || (V == 8 && G > 4) || V == 16) ? 24 : 32) / kSpmmWarps;
+}
+
+// One pass of one piece of a long row (rb_pr, spmm_pieces_pass): the row's
+// nonzeros [b_pass, b_pass+1) of the piece, split over the P = 32/G slots in
+// batches of 32 (slot s takes batch positions s, s+P, ...), 4 sixteen-byte
+// or wider loads (8 narrower ones) in flight per lane, the next batch's
+// indices loading meanwhile; then the slots' sums folded and left to
+// finish_piece.  The same arithmetic as the row walk's split path, without
+// its row bookkeeping.
+template <typename BT, int V, int G>
+__device__ __forceinline__ void spmm_piece_unit(const SpmmArgs<BT> &a, long long w, int slab,
+                                                int lane, int pass) {
+  constexpr int P = 32 / G;
+  constexpr int UL = V * (int)sizeof(BT) >= 16 ? 4 : 8;
+  constexpr int UB = G < UL ? G : UL;  // steps of a batch in flight per lane
+  using D = Dense<BT, V>;
+  const unsigned FULL = 0xffffffffu;
+  const int slot = lane / G, gl = lane & (G - 1);
+  const int col0 = slab * (G * V) + gl * V;
+  const bool active = col0 < a.N;
+  const uint64_t pol = l2_policy(a.l2_hints);
+  const BT *Bc = a.B + (active ? col0 : 0);  // lanes past N load column 0, never store
+  const unsigned ldb = (unsigned)a.ldb;
+  if (w < a.piece_multi ? w >= (long long)__ldg(a.piece_count)
+                        : w - a.piece_multi >= (long long)__ldg(a.piece_count + 1))
+    return;
+  const int2 pc = __ldg(a.pieces + w);
+  const int row = pc.x;
+  int y0 = pc.y;
+  int y1 = min(pc.y + a.piece_len, __ldg(a.row_ptr + row + 1));
+  if (a.piece_parts > 1) {
+    const long long Kp = ((long long)a.K + a.piece_parts - 1) / a.piece_parts;
+    for (int q = 1; q <= pass; ++q) y0 = warp_lower_bound(a.col, y0, y1, q * Kp, lane);
+    if (pass + 1 < a.piece_parts) y1 = warp_lower_bound(a.col, y0, y1, (pass + 1) * Kp, lane);
+  }
+  float acc[V];
+  zero<V>(acc);
+  int mc = lane < y1 - y0 ? ld_stream(a.col + y0 + lane) : 0;
+  float mv = lane < y1 - y0 ? ld_val(a.val, y0 + lane) : 0.0f;
+  for (int p = y0; p < y1; p += 32) {
+    const int nb = y1 - p < 32 ? y1 - p : 32;
+    const int nxt = p + 32;
+    const int mcn = lane < y1 - nxt ? ld_stream(a.col + nxt + lane) : 0;
+    const float mvn = lane < y1 - nxt ? ld_val(a.val, nxt + lane) : 0.0f;
+#pragma unroll
+    for (int s0 = 0; s0 < G; s0 += UB) {
+      if (s0 * P >= nb) break;  // warp-uniform
+      typename D::raw_t b[UB];
+      float vv[UB];
+#pragma unroll
+      for (int u = 0; u < UB; ++u) {
+        const int t = (s0 + u) * P + slot;
+        const bool ok = t < nb;
+        const int j = __shfl_sync(FULL, mc, ok ? t : 0);
+        const float v = __shfl_sync(FULL, mv, ok ? t : 0);
+        vv[u] = ok ? v : 0.0f;
+        b[u] = D::load(Bc + (size_t)(unsigned)j * ldb, pol);
+      }
+#pragma unroll
+      for (int u = 0; u < UB; ++u) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc[v] = fmaf(vv[u], D::get(b[u], v), acc[v]);
+      }
+    }
+    mc = mcn;
+    mv = mvn;
+  }
+  bool owner;
+  const int first = fold_slots_scatter<G, V>(acc, lane, owner);
+  finish_piece<BT, fold_scatter_count<G, V>()>(a, w, row, pc.y, slab,
+                                               (a.N + G * V - 1) / (G * V), acc,
+                                               active && owner, col0 + first, lane, pass);
+}
+
+// rb_pr's pieces in piece_parts passes (a launch of their own, before the row
+// blocks): items (pass, slab, piece) in that order, each warp taking the next
+// item from a counter, so that the grid works through one (pass, slab) at a
+// time and its gathers stay within one range of B's rows of one slab (Kp x W
+// elements) while it runs.
+template <typename BT, int V, int G>
+__device__ __forceinline__ void spmm_pieces_pass(const SpmmArgs<BT> &a, int lane) {
+  const long long n0 = min((long long)__ldg(a.piece_count), a.piece_multi);
+  const long long n1 = min((long long)__ldg(a.piece_count + 1), a.piece_cap - a.piece_multi);
+  const long long total = n0 + n1;
+  const long long slabs = (a.N + G * V - 1) / (G * V);
+  const unsigned long long items = (unsigned long long)(total * slabs * a.piece_parts);
+  for (;;) {
+    unsigned long long t = 0;
+    if (lane == 0) t = atomicAdd(a.piece_queue, 1ull);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= items) return;
+    const long long i = (long long)(t % (unsigned long long)total);
+    const long long ps = (long long)(t / (unsigned long long)total);
+    spmm_piece_unit<BT, V, G>(a, i < n0 ? i : a.piece_multi + (i - n0), (int)(ps % slabs), lane,
+                              (int)(ps / slabs));
+  }
+}
+
+// The pieces' passes as a kernel of their own: a persistent grid of
+// spmm_min_ctas CTAs per multiprocessor (the row blocks' occupancy).
+template <typename BT, int V, int G>
+__global__ void __launch_bounds__(kSpmmCta, spmm_min_ctas<V, G, false>())
+    spmm_pieces_kernel(SpmmArgs<BT> a) {
+  spmm_pieces_pass<BT, V, G>(a, threadIdx.x & 31);
 }
 
 template <typename BT, int V, int G, bool ROWS, int WALK = kWalkRows>

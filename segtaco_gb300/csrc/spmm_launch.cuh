@@ -36,6 +36,8 @@ template <typename BT> inline SpmmArgs<BT> make_spmm_args(const SpmmLaunch &L) {
   a.piece_multi = L.piece_multi;
   a.piece_ld = L.piece_ld;
   a.piece_len = L.piece_len;
+  a.piece_parts = L.piece_parts > 1 ? L.piece_parts : 1;
+  a.piece_queue = L.piece_queue;
   return a;
 }
 
@@ -180,4 +182,32 @@ inline dim3 spmm_grid(const SpmmLaunch &L) {
     }                                                                                     \
     return check_launch(#NAME);                                                           \
   }                                                                                       \
+  }
+
+// The pieces' launcher of one dense type (spmm_<dtype>_pieces.cu): the row
+// walk's (V, G) pairs with at least two slots.
+#define SEGTACO_PIECES_CASE(BT, V, G)                                                    \
+  case V * 100 + G:                                                                      \
+    spmm_pieces_kernel<BT, V, G>                                                         \
+        <<<spmm_min_ctas<V, G, false>() * device_sms(), kSpmmCta, 0, s>>>(a);            \
+    break;
+#define SEGTACO_PIECES_VG(X, BT)                                                         \
+  X(BT, 1, 1) X(BT, 1, 2) X(BT, 1, 4) X(BT, 1, 8) X(BT, 1, 16)                           \
+  X(BT, 2, 1) X(BT, 2, 2) X(BT, 2, 4) X(BT, 2, 8) X(BT, 2, 16)                           \
+  X(BT, 4, 1) X(BT, 4, 2) X(BT, 4, 4) X(BT, 4, 8) X(BT, 4, 16)                           \
+  X(BT, 8, 1) X(BT, 8, 2) X(BT, 8, 4) X(BT, 8, 8) X(BT, 8, 16)
+#define SEGTACO_DEFINE_PIECES_LAUNCHER(NAME, BT, EXTRA)                                  \
+  namespace segtaco {                                                                    \
+  int NAME(const SpmmLaunch &L, cudaStream_t s) {                                        \
+    const SpmmArgs<BT> a = make_spmm_args<BT>(L);                                        \
+    SEGTACO_TRY(check_cuda(cudaMemsetAsync(L.piece_queue, 0, sizeof(unsigned long long), s), \
+                           "cudaMemsetAsync"));                                          \
+    switch (L.V * 100 + L.G) {                                                           \
+      SEGTACO_PIECES_VG(SEGTACO_PIECES_CASE, BT)                                         \
+      EXTRA                                                                              \
+      default:                                                                           \
+        return set_error(SEGTACO_EUNSUPPORTED, #NAME ": no variant V=%d G=%d", L.V, L.G); \
+    }                                                                                    \
+    return check_launch(#NAME);                                                          \
+  }                                                                                      \
   }

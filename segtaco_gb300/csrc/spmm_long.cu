@@ -127,11 +127,13 @@ __global__ void long_rows_list_kernel(const int *__restrict__ row_ptr, int M, in
 // rb_pr: thread per row; a row of >= long_row nonzeros appends its pieces of
 // piece_len nonzeros: several (consecutive entries of the front part, the
 // counters of its first piece cleared, one per column slab) or one (the back
-// part, from entry `multi`).
+// part, from entry `multi`; its counters cleared too when the pieces run in
+// several passes, `all_ctr`).
 __global__ void long_pieces_list_kernel(const int *__restrict__ row_ptr, int M, int long_row,
                                         int piece_len, int2 *__restrict__ pieces,
                                         long long multi, long long cap,
-                                        unsigned *__restrict__ ctr, int slabs, int *count) {
+                                        unsigned *__restrict__ ctr, int slabs, int *count,
+                                        bool all_ctr) {
   const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= M) return;
   const int b = __ldg(row_ptr + r);
@@ -140,7 +142,11 @@ __global__ void long_pieces_list_kernel(const int *__restrict__ row_ptr, int M, 
   const int n = (len + piece_len - 1) / piece_len;
   if (n == 1) {
     const long long i = multi + atomicAdd(count + 1, 1);
-    if (i < cap) pieces[i] = make_int2((int)r, b);
+    if (i < cap) {
+      pieces[i] = make_int2((int)r, b);
+      if (all_ctr)
+        for (int sl = 0; sl < slabs; ++sl) ctr[i * slabs + sl] = 0u;
+    }
     return;
   }
   const long long i = atomicAdd(count, n);
@@ -414,7 +420,9 @@ LongFork *long_fork(cudaStream_t s) {
   return &t_fork;
 }
 
-int sm_count() {
+}  // namespace
+
+int device_sms() {
   static std::atomic<int> counts[kForkDevices];
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kForkDevices) {
@@ -432,8 +440,6 @@ int sm_count() {
   return n;
 }
 
-}  // namespace
-
 int launch_long_rows_list(const int *row_ptr, int M, long long nnz, int long_row, int *list,
                           int *counters, cudaStream_t s) {
   long long cap_hi, cap_lo;
@@ -446,19 +452,19 @@ int launch_long_rows_list(const int *row_ptr, int M, long long nnz, int long_row
 }
 
 int launch_long_pieces_list(const int *row_ptr, int M, long long nnz, int long_row, int piece_len,
-                            int slabs, int W, int *pieces, int *count, cudaStream_t s) {
+                            int slabs, int W, int parts, int *pieces, int *count, cudaStream_t s) {
   SEGTACO_TRY(check_cuda(cudaMemsetAsync(count, 0, 2 * sizeof(int), s), "cudaMemsetAsync"));
   if (M <= 0) return SEGTACO_OK;
-  const PieceLayout pl = piece_layout(nnz, long_row, piece_len, slabs, W);
+  const PieceLayout pl = piece_layout(nnz, long_row, piece_len, slabs, W, parts);
   long_pieces_list_kernel<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(
       row_ptr, M, long_row, piece_len, reinterpret_cast<int2 *>(pieces), pl.multi, pl.cap,
-      reinterpret_cast<unsigned *>(pieces + pl.ctr), slabs, count);
+      reinterpret_cast<unsigned *>(pieces + pl.ctr), slabs, count, parts > 1);
   return check_launch("long_pieces_list_kernel");
 }
 
 int launch_spmm_long_rows(const SpmmLaunch &L, const int *list, int *counters, cudaStream_t s) {
   const bool bf16 = L.dtype == SEGTACO_BF16;
-  const int sms = sm_count();
+  const int sms = device_sms();
   // The work queue is cleared before the fork, so that the long-row kernel is
   // the side stream's first operation and reaches the GPU before the
   // row-block kernel.

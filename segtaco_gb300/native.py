@@ -52,14 +52,14 @@ class Config(C.Structure):
     """segtaco_config: zero fields mean automatic."""
     _fields_ = [("schedule", C.c_int32), ("col_tile", C.c_int32), ("vec", C.c_int32),
                 ("rows_per_unit", C.c_int32), ("items_per_unit", C.c_int32),
-                ("flags", C.c_uint32), ("depth", C.c_int32)]
+                ("flags", C.c_uint32), ("depth", C.c_int32), ("k_parts", C.c_int32)]
 
     @classmethod
     def make(cls, schedule=AUTO, col_tile=0, vec=0, rows_per_unit=0, items_per_unit=0,
-             flags=0, depth=0):
+             flags=0, depth=0, k_parts=0):
         if isinstance(schedule, str):
             schedule = SCHEDULES[schedule]
-        return cls(schedule, col_tile, vec, rows_per_unit, items_per_unit, flags, depth)
+        return cls(schedule, col_tile, vec, rows_per_unit, items_per_unit, flags, depth, k_parts)
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

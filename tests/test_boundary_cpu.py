@@ -178,10 +178,29 @@ def test_workspace_and_heuristic(native_lib):
     multi = 2 * 2 * 10**7 // 4096 + 1
     cap = multi + 2 * 10**7 // 512 + 1  # default threshold for rb_pr: 512
     part = (2 * cap + 4 * multi + 63) // 64 * 64
-    c = N.Config.make(schedule="rb_pr", flags=LR)
+    c = N.Config.make(schedule="rb_pr", flags=LR, k_parts=1)
     assert L.segtaco_spmm_workspace_size(10**6, 10**6, 2 * 10**7, 128, N.F32, C.byref(c),
                                          C.byref(out)) == N.OK
     assert out.value == ((part + multi * 128) * 4 + 255) // 256 * 256 + 256
+    c = N.Config.make(schedule="rb_pr", flags=LR)  # one pass by default
+    assert L.segtaco_spmm_workspace_size(10**6, 10**6, 2 * 10**7, 128, N.F32, C.byref(c),
+                                         C.byref(out)) == N.OK
+    assert out.value == ((part + multi * 128) * 4 + 255) // 256 * 256 + 256
+    # two passes over B's rows: pieces of 2048, every entry with counters and
+    # two partial rows
+    multi = 2 * 2 * 10**7 // 2048 + 1
+    cap = multi + 2 * 10**7 // 512 + 1
+    part = (2 * cap + 4 * cap + 63) // 64 * 64
+    c = N.Config.make(schedule="rb_pr", flags=LR, k_parts=2)
+    assert L.segtaco_spmm_workspace_size(10**6, 10**6, 2 * 10**7, 128, N.F32, C.byref(c),
+                                         C.byref(out)) == N.OK
+    assert out.value == ((part + cap * 2 * 128) * 4 + 255) // 256 * 256 + 256
+    name = C.create_string_buffer(256)
+    for k, want_parts in ((0, 1), (2, 2), (9, 8)):
+        c = N.Config.make(schedule="rb_pr", flags=LR, k_parts=k)
+        assert L.segtaco_spmm_plan_name(10**6, 10**6, 2 * 10**7, 128, N.F32, None, 128,
+                                        C.byref(c), name, 256) == N.OK
+        assert name.value.decode().endswith(" parts=%d" % want_parts)
     c = N.Config.make(schedule="rb_pr", flags=LR, col_tile=32, vec=4)
     name = C.create_string_buffer(256)
     assert L.segtaco_spmm_plan_name(10**6, 10**6, 2 * 10**7, 128, N.F32, None, 128, C.byref(c),

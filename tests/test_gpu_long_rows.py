@@ -224,3 +224,99 @@ def test_rb_sr_narrow_slabs_bit_identical(cuda, A, col_tile):
     Ad, Bd = dev(A), torch.from_numpy(B).cuda()
     got = run(Ad, Bd, 128, "rb_sr", col_tile=col_tile)
     assert np.array_equal(got, rowseq(A, B))
+
+
+def _with_long_rows_shuffled(A, seed):
+    """A copy of A whose rows of >= 512 nonzeros hold their (column, value)
+    pairs in a random order (CSR does not require sorted columns)."""
+    rng = np.random.default_rng(seed)
+    col, val = A.col.copy(), A.val.copy()
+    rp = A.row_ptr
+    for r in np.nonzero(A.row_lengths() >= 512)[0]:
+        p = rng.permutation(rp[r + 1] - rp[r]) + rp[r]
+        col[rp[r]:rp[r + 1]] = A.col[p]
+        val[rp[r]:rp[r + 1]] = A.val[p]
+    return synth.CSR(A.row_ptr, col, val, A.M, A.K)
+
+
+@pytest.mark.parametrize("parts,n", [(2, 128), (3, 64), (8, 40), (2, 200), (5, 96)])
+def test_rb_pr_pieces_in_passes(cuda, A, parts, n):
+    """rb_pr's pieces in k_parts passes over ranges of B's rows (a launch of
+    their own before the row blocks): every (piece, pass) leaves a partial row,
+    summed in order, so reruns are bit-identical; thresholds that make rows of
+    one piece (stored through the partials too) and of several."""
+    B = synth.dense(A.K, n, seed=90 + parts)
+    Ad, Bd = dev(A), torch.from_numpy(B).cuda()
+    ref = spmm_ref(A, B)
+    for threshold in (0, 300, 4097):
+        cfg = dict(items_per_unit=threshold, k_parts=parts)
+        assert ops.plan_name(Ad, Bd, N.Config.make(schedule="rb_pr", flags=N.FLAG_LONG_ROWS,
+                                                   **cfg)).endswith(" parts=%d" % parts)
+        got = run(Ad, Bd, n, "rb_pr", **cfg)
+        assert_spmm_close(got, A, B, ref=ref)
+        assert np.array_equal(got, run(Ad, Bd, n, "rb_pr", **cfg))
+
+
+def test_rb_pr_pieces_in_passes_bf16_and_unsorted(cuda, A):
+    """bf16 B in two passes; long rows with unsorted columns (each pass's range
+    of a piece then holds columns of every range: still every nonzero once)."""
+    bits = synth.to_bf16_bits(synth.dense(A.K, 64, seed=95))
+    got = run(dev(A), to_torch_bf16(bits), 64, "rb_pr", k_parts=2)
+    assert_spmm_close(got, A, bits, bf16=True)
+    U = _with_long_rows_shuffled(A, 96)
+    B = synth.dense(U.K, 128, seed=97)
+    Ud, Bd = dev(U), torch.from_numpy(B).cuda()
+    for parts in (2, 4):
+        got = run(Ud, Bd, 128, "rb_pr", k_parts=parts)
+        assert_spmm_close(got, U, B)
+        assert np.array_equal(got, run(Ud, Bd, 128, "rb_pr", k_parts=parts))
+
+
+def test_rb_pr_pieces_in_passes_one_sided_rows(cuda):
+    """Long rows whose columns all fall in one pass's range (the other passes
+    see an empty range and leave zero partial rows), one across a range edge
+    and one starting exactly on it, a short row of that edge column alone, and
+    K not a multiple of the pass count; partition-ready reruns and a graph
+    replay."""
+    rng = np.random.default_rng(98)
+    M, K = 30_000, 10_007
+    lengths = rng.binomial(70, 0.5, M)
+    rows = np.repeat(np.arange(M, dtype=np.int64), lengths)
+    keys = [np.unique(rows * K + rng.integers(0, K, rows.size))]
+    edge = (K + 2) // 3  # the first column of pass 1 of 3
+    special = {5: np.arange(0, 3000), 6: np.arange(K - 2500, K), 7: np.arange(edge - 700, edge + 700),
+               8: np.array([edge]), 9: np.arange(edge, edge + 2000)}
+    for r in special:
+        keys[0] = keys[0][keys[0] // K != r]
+    keys += [r * K + c for r, c in special.items()]
+    A = synth._from_keys(np.sort(np.concatenate(keys)), M, K, rng)
+    assert A.nnz >= 1_000_000
+    B = synth.dense(K, 96, seed=99)
+    Ad, Bd = dev(A), torch.from_numpy(B).cuda()
+    ref = spmm_ref(A, B)
+    cfg = N.Config.make(schedule="rb_pr", flags=N.FLAG_LONG_ROWS, k_parts=3)
+    ws = torch.empty(ops.spmm_workspace_size(Ad, 96, N.F32, cfg), dtype=torch.uint8,
+                     device="cuda")
+    C_ = torch.full((A.M, 96), float("nan"), device="cuda")
+    ops.spmm_partition(Ad, C_, cfg, ws)
+    ready = N.Config.make(schedule="rb_pr", flags=N.FLAG_LONG_ROWS | N.FLAG_PARTITION_READY,
+                          k_parts=3)
+    first = None
+    for _ in range(3):
+        C_.fill_(float("nan"))
+        ops.spmm(Ad, Bd, C_out=C_, config=ready, workspace=ws)
+        torch.cuda.synchronize()
+        got = C_.cpu().numpy()
+        if first is None:
+            first = got
+            assert_spmm_close(got, A, B, ref=ref)
+        assert np.array_equal(got, first)
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        ops.spmm(Ad, Bd, C_out=C_, config=cfg, workspace=ws)
+    for _ in range(2):
+        C_.fill_(float("nan"))
+        g.replay()
+        torch.cuda.synchronize()
+        assert np.array_equal(C_.cpu().numpy(), first)
