@@ -63,15 +63,54 @@ __global__ void batch_partition_kernel(const BatchPartition *__restrict__ parts,
   // Global rows t over every problem, M + 1 each (the last is the problem's
   // tail); row t writes the chunk edges inside it (merge_path_store_row).  A
   // thread walks kBatchPartRows consecutive rows, possibly across problems.
-  const long long t0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * kBatchPartRows;
+  // The block's first problem comes from one search; a thread whose rows lie
+  // in one problem loads their row_ptr entries together, before any store.
+  __shared__ int s_part;
+  const long long tb = (long long)blockIdx.x * blockDim.x * kBatchPartRows;
+  if (threadIdx.x == 0) {
+    int lo = 0, hi = nparts - 1;  // last part with row_begin <= tb
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (parts[mid].row_begin <= tb)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    s_part = lo;
+  }
+  __syncthreads();
+  const long long t0 = tb + (long long)threadIdx.x * kBatchPartRows;
   if (t0 >= total_rows) return;
-  int lo = 0, hi = nparts - 1;  // last part with row_begin <= t0
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (parts[mid].row_begin <= t0)
-      lo = mid;
-    else
-      hi = mid - 1;
+  int lo = s_part;
+  while (lo + 1 < nparts && parts[lo + 1].row_begin <= t0) ++lo;
+  {
+    const BatchPartition bp = parts[lo];
+    const long long r0 = t0 - bp.row_begin;
+    if (r0 + kBatchPartRows - 1 <= bp.M) {
+      // rows r0 .. r0+3 all in this problem: e[k] = e_{r0+k-1} = row_ptr[r0+k] + r0 + k
+      const bool small = (long long)bp.M + bp.nnz + bp.D < 0x7fffffffLL;
+      long long e[kBatchPartRows + 1];
+#pragma unroll
+      for (int k = 0; k <= kBatchPartRows; ++k) {
+        const long long r = r0 + k;
+        e[k] = (r > 0 && r <= bp.M) ? (long long)__ldg(bp.row_ptr + r) + r : 0;
+      }
+      long long c_lo = ceil_div_pos(e[0], bp.D, small);
+#pragma unroll
+      for (int k = 0; k < kBatchPartRows; ++k) {
+        const long long r = r0 + k;
+        if (r < bp.M) {
+          const long long nxt = ceil_div_pos(e[k + 1], bp.D, small);
+          merge_path_store_row(bp.row_ptr, bp.M, bp.nnz, bp.D, bp.nchunks, r, c_lo, nxt - 1,
+                               bp.px, bp.py, bp.C, bp.ldc, bp.N);
+          c_lo = nxt;
+        } else {
+          merge_path_store_row(bp.row_ptr, bp.M, bp.nnz, bp.D, bp.nchunks, r, c_lo, bp.nchunks,
+                               bp.px, bp.py, bp.C, bp.ldc, bp.N);
+        }
+      }
+      return;
+    }
   }
   for (int k = 0; k < kBatchPartRows; ++k) {
     const long long t = t0 + k;
