@@ -251,12 +251,9 @@ template <typename BT> struct Window {
 
 // Walk one unit (merge-path chunk or row block) `w` over column slab `slab`.
 // The body of every SpMM kernel below (single problem or batched).
-// pass >= 0 (rb_pr pieces in several passes, spmm_pieces_pass): piece `w`
-// restricted to the nonzeros of that pass's range of B's rows.
 template <typename BT, int V, int G, bool ROWS, bool DEEP, bool WIN = false>
 __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long w, int slab,
-                                               int lane, Window<BT> win = Window<BT>(),
-                                               int pass = -1) {
+                                               int lane, Window<BT> win = Window<BT>()) {
   constexpr int P = 32 / G;                 // slots
   // Rows with >= LONG nonzeros are split over the slots (LONG <= 32, so a
   // short row always fits one batch).
@@ -285,7 +282,6 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
   };
 
   int x0, x1, y0, y1;
-  int py0 = 0;  // a piece's first nonzero
   bool head_split = false, tail_open = false;
   if (ROWS) {
     if (w < a.piece_cap) {
@@ -296,17 +292,8 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
         return;
       const int2 pc = __ldg(a.pieces + w);
       x0 = x1 = pc.x;
-      py0 = y0 = pc.y;
+      y0 = pc.y;
       y1 = min(pc.y + a.piece_len, __ldg(a.row_ptr + pc.x + 1));
-      if (pass >= 0) {
-        // this pass's range [b_pass, b_pass+1) of the piece: b_0 = y0, b_R =
-        // y1, b_p the first nonzero of column >= p*Kp at or after b_p-1
-        const long long Kp = ((long long)a.K + a.piece_parts - 1) / a.piece_parts;
-        int lo = y0;
-        for (int q = 1; q <= pass; ++q) lo = warp_lower_bound(a.col, lo, y1, q * Kp, lane);
-        if (pass + 1 < a.piece_parts) y1 = warp_lower_bound(a.col, lo, y1, (pass + 1) * Kp, lane);
-        y0 = lo;
-      }
       head_split = tail_open = true;
     } else {
       const long long r0 = (w - a.piece_cap) * a.rows_per_unit;
@@ -452,10 +439,9 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
         bool owner;
         const int first = fold_slots_scatter<G, V>(acc, lane, owner);
         if (ROWS && piece) {
-          finish_piece<BT, fold_scatter_count<G, V>()>(a, w, cur, py0, slab,
+          finish_piece<BT, fold_scatter_count<G, V>()>(a, w, cur, y0, slab,
                                                        (a.N + G * V - 1) / (G * V), acc,
-                                                       active && owner, col0 + first, lane,
-                                                       pass < 0 ? 0 : pass);
+                                                       active && owner, col0 + first, lane, 0);
         } else if (active && owner) {
           const bool edge = (cur == x0 && head_split) || (cur == x1 && tail_open);
           constexpr int R = fold_scatter_count<G, V>();
@@ -463,8 +449,8 @@ __device__ __forceinline__ void spmm_walk_unit(const SpmmArgs<BT> &a, long long 
                                             edge);
         }
       } else if (ROWS && piece) {
-        finish_piece<BT, V>(a, w, cur, py0, slab, (a.N + G * V - 1) / (G * V), acc, active, col0,
-                            lane, pass < 0 ? 0 : pass);
+        finish_piece<BT, V>(a, w, cur, y0, slab, (a.N + G * V - 1) / (G * V), acc, active, col0,
+                            lane, 0);
       } else if (active) {
         float *dst = a.C + (long long)cur * a.ldc + col0;
         if ((cur == x0 && head_split) || (cur == x1 && tail_open))
