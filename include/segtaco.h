@@ -126,8 +126,9 @@ typedef struct segtaco_config {
                              shared memory for the whole CTA, each column
                              still summed in storage order, beside the
                              row-block kernel.  rb_pr: split into pieces of
-                             512 nonzeros that warps of the row-block launch
-                             take over the same column slabs; each piece's
+                             4096 nonzeros (2048 with k_parts > 1) that warps
+                             of the row-block launch take over the same
+                             column slabs; each piece's
                              partial row goes to the workspace and the last
                              piece of a row sums them in piece order, so the
                              result does not vary from run to run          */
