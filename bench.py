@@ -323,18 +323,25 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def _b_dtype(N_, Bd):
+    """The dense operand's type code (bf16 B travels as bf16 or int16 bits)."""
+    import torch
+    return N_.BF16 if Bd.dtype in (torch.bfloat16, torch.int16) else N_.F32
+
+
 def time_spmm(ops, N_, Ad, Bd, Cd, cfg, ws, stream, steps, warmup):
     """Per-step device time and product-kernel time (ms) via events on `stream`."""
     import torch
     cfg_ready = N_.Config.make(**{**cfg.as_dict(), "flags": cfg.flags | N_.FLAG_PARTITION_READY})
+    dt = _b_dtype(N_, Bd)
     for _ in range(warmup):
-        ops.spmm_partition(Ad, Cd, cfg, ws, stream=stream)
+        ops.spmm_partition(Ad, Cd, cfg, ws, b_dtype=dt, stream=stream)
         ops.spmm(Ad, Bd, C_out=Cd, config=cfg_ready, workspace=ws, stream=stream)
     torch.cuda.synchronize()
     ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
     for i in range(steps):
         ev[i][0].record(stream)
-        ops.spmm_partition(Ad, Cd, cfg, ws, stream=stream)
+        ops.spmm_partition(Ad, Cd, cfg, ws, b_dtype=dt, stream=stream)
         ev[i][1].record(stream)
         ops.spmm(Ad, Bd, C_out=Cd, config=cfg_ready, workspace=ws, stream=stream)
         ev[i][2].record(stream)
@@ -350,9 +357,10 @@ def time_spmm_graph(ops, N_, Ad, Bd, Cd, cfg, ws, stream, reps, warmup):
     segTACO's timer brackets only its own launches)."""
     import torch
     cfg_ready = N_.Config.make(**{**cfg.as_dict(), "flags": cfg.flags | N_.FLAG_PARTITION_READY})
+    dt = _b_dtype(N_, Bd)
 
     def step():
-        ops.spmm_partition(Ad, Cd, cfg, ws, stream=stream)
+        ops.spmm_partition(Ad, Cd, cfg, ws, b_dtype=dt, stream=stream)
         ops.spmm(Ad, Bd, C_out=Cd, config=cfg_ready, workspace=ws, stream=stream)
     with torch.cuda.stream(stream):
         for _ in range(warmup):
