@@ -59,3 +59,15 @@ def test_result_line_is_compact():
     assert len(json.dumps(s, separators=(",", ":"))) < 2200
     assert s["batched"]["speedup_vs_per_call_graph"] == 3.2
     assert set(s["schedules"]) == {"rb_sr", "rb_pr", "eb_sr", "eb_pr"}
+
+
+def test_launches_per_step():
+    """The launch count a step claims follows the plan: merge path + product;
+    rb_pr's list + row blocks (+ the pieces' passes); rb_sr's list + long-row
+    CTAs + row blocks; a plain row-block product."""
+    P = "rb_pr pieces V=8 G=4 W=32 slabs=4 walk=0 halo=-1 rows_per_unit=64 parts=%d"
+    assert bench.launches_per_step(True, 4096, "eb_pr chunks V=8 G=4 parts=1") == 2
+    assert bench.launches_per_step(False, 4096, P % 1) == 2
+    assert bench.launches_per_step(False, 4096, P % 2) == 3
+    assert bench.launches_per_step(False, 4096, "rb_sr long_rows V=4 G=32 parts=1") == 3
+    assert bench.launches_per_step(False, 0, "rb_pr rows V=8 G=4 parts=1") == 1
