@@ -1,6 +1,7 @@
 """bench.py's algorithmic bytes (the roofline numerator) and workloads: the
 SpMM formula nnz*(4+4) + (M+1)*4 + K*N*s_B + M*N*4 at the configurations'
-sizes, and the workload names the bench and the driver use."""
+sizes, the workload names bench.py accepts, and the launches a timed step
+claims."""
 import os
 import sys
 
