@@ -1043,6 +1043,31 @@ def launches_per_step(eb, ws_need, plan):
     return 3 if ws_need else 1
 
 
+RESULT_KEYS = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+               "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config",
+               "roofline", "gpu_launches", "e2e", "cpu_baseline", "clocks")
+
+
+def result_line(detail):
+    """The result line (printed last): the contract's keys and a compact
+    summary, well inside a 3 KB tail; the gather and flop figures, the clock
+    sample counts and the CPU baseline's one-thread sample live in the detail
+    line."""
+    line = {k: detail[k] for k in RESULT_KEYS}
+    if isinstance(line["roofline"], dict):
+        line["roofline"] = {k: v for k, v in line["roofline"].items()
+                            if k not in ("gathered_bytes", "gather_GBps", "flops", "tflops")}
+    if isinstance(line["clocks"], dict):
+        line["clocks"] = {k: v for k, v in line["clocks"].items()
+                          if k not in ("samples", "interval_ms", "nvml_samples")}
+    if isinstance(line["cpu_baseline"], dict) and "one_thread" in line["cpu_baseline"]:
+        line["cpu_baseline"] = dict(line["cpu_baseline"])
+        line["cpu_baseline"]["one_thread"] = {
+            "value": line["cpu_baseline"]["one_thread"].get("value")}
+    line["summary"] = compact_summary(detail)
+    return line
+
+
 def compact_summary(d):
     """The headline's context in a few hundred bytes: per-schedule kernel ms,
     roofline fraction and error vs FP64; segTACO's own GPU kernels and
@@ -1053,7 +1078,7 @@ def compact_summary(d):
     if d.get("schedules"):
         out["schedules"] = {k: [v["kernel_ms"], v["roofline_frac"], float("%.2g" % v["max_err_vs_fp64"])]
                             for k, v in d["schedules"].items()}
-        out["schedules_fields"] = ["kernel_ms", "roofline_frac", "max_err_vs_fp64"]
+        out["schedules_fields"] = ["kernel_ms", "frac", "err_vs_fp64"]
     v = d.get("power_law_10m")
     if v:
         out["power_law_10m_ms"] = {k: x["kernel_ms"] for k, x in v["schedules"].items()}
@@ -1077,17 +1102,16 @@ def compact_summary(d):
     if b:
         out["batched"] = {"speedup_vs_per_call_graph": b["speedup_vs_per_call"],
                           "per_call_graph_ms": b["per_call_graph_ms"],
-                          "per_call_python_ms": b["per_call_ms"],
                           "batched_graph_ms": b["batched_graph_ms"],
                           "max_err_vs_fp64": float("%.2g" % b["max_err_vs_fp64"])}
     sv = d.get("served")
     if sv:
         def one(x):
-            return [x["batched"]["requests_per_s"], x["per_call"]["requests_per_s"],
-                    x["batched"]["p50_us"], x["batched"]["p99_us"], x["per_call"]["p99_us"],
-                    x["capacity_vs_per_call"]]
-        out["served_fields"] = ["req_per_s", "per_call_req_per_s", "p50_us", "p99_us",
-                                "per_call_p99_us", "capacity_vs_per_call"]
+            return [round(x["batched"]["requests_per_s"]), round(x["per_call"]["requests_per_s"]),
+                    round(x["batched"]["p50_us"]), round(x["batched"]["p99_us"]),
+                    round(x["per_call"]["p99_us"]), round(x["capacity_vs_per_call"], 2)]
+        out["served_fields"] = ["rps", "per_call_rps", "p50_us", "p99_us", "per_call_p99_us",
+                                "capacity_x"]
         out["served"] = {"fp32_host": one(sv)}
         for k, n in (("bf16_operands", "bf16_host"), ("device_operands", "fp32_device")):
             if sv.get(k):
@@ -1102,7 +1126,7 @@ def compact_summary(d):
                 err = x.get("max_err_vs_fp64", x.get("max_err_vs_fp64_bf16_values"))
                 out["side_ops"][k] = [x["ms"], x["roofline_frac"]] + (
                     [float("%.2g" % err)] if err is not None else [])
-        out["side_ops_fields"] = ["ms", "roofline_frac", "max_err_vs_fp64"]
+        out["side_ops_fields"] = ["ms", "frac", "err_vs_fp64"]
     return out
 
 
@@ -1323,20 +1347,7 @@ def run_ours(args, world, rank, local):
         print("# detail " + json.dumps(detail), flush=True)
         # ... then the result line last and compact, so that a reader of the
         # last few KB of output sees it whole.
-        line = {k: detail[k] for k in (
-            "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
-            "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config", "roofline",
-            "gpu_launches", "e2e", "cpu_baseline", "clocks")}
-        # the result line stays well inside a 3 KB tail: the gather and flop
-        # figures and the CPU baseline's one-thread sample live in the detail line
-        line["roofline"] = {k: v for k, v in line["roofline"].items()
-                            if k not in ("gathered_bytes", "flops", "tflops")}
-        if isinstance(line["cpu_baseline"], dict) and "one_thread" in line["cpu_baseline"]:
-            line["cpu_baseline"] = dict(line["cpu_baseline"])
-            line["cpu_baseline"]["one_thread"] = {
-                "value": line["cpu_baseline"]["one_thread"].get("value")}
-        line["summary"] = compact_summary(detail)
-        print(json.dumps(line, separators=(",", ":")), flush=True)
+        print(json.dumps(result_line(detail), separators=(",", ":")), flush=True)
 
 
 def main():

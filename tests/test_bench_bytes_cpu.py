@@ -72,3 +72,73 @@ def test_launches_per_step():
     assert bench.launches_per_step(False, 4096, P % 2) == 3
     assert bench.launches_per_step(False, 4096, "rb_sr long_rows V=4 G=32 parts=1") == 3
     assert bench.launches_per_step(False, 0, "rb_pr rows V=8 G=4 parts=1") == 1
+
+
+def _sample_detail():
+    """A detail record shaped like the bench's, with long-ish numbers."""
+    S = ("rb_sr", "rb_pr", "eb_sr", "eb_pr")
+
+    def served_arm():
+        return {"requests_per_s": 19759.4321, "p50_us": 121352.8123, "p99_us": 164767.4123}
+
+    def served():
+        return {"batched": served_arm(), "per_call": served_arm(), "capacity_vs_per_call": 4.1473,
+                "max_err_vs_fp64": 1.8123e-07}
+    return {
+        "metric": "SpMM HBM GB/s (% of roofline)", "value": 1081.9, "unit": "GB/s", "n_gpus": 1,
+        "steps": 20, "warmup": 5, "ms_per_step": 1.1023, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded numpy PCG64)",
+        "config": {"workload": "power-law SpMM: A 1Mx1M Zipf(1.8) cap 50000, 2% empty rows, "
+                               "N=128, fp32", "M": 1000000, "K": 1000000, "nnz": 20567850,
+                   "N": 128, "schedule": "eb_pr", "col_tile": 32, "items_per_unit": 512,
+                   "l2_hints": True,
+                   "l2": "no flush: A 169 MB, B 512 MB, C 512 MB each exceed the 129 MB L2",
+                   "parallelism": "replicas x1"},
+        "roofline": {"bound": "hbm", "achieved": 1096.4, "peak": 6796.5, "unit": "GB/s",
+                     "frac": 0.1613, "traffic": 6029844224, "kernel": "spmm_eb_pr_kernel",
+                     "gathered_bytes": 10530739200, "gather_GBps": 9681.6, "flops": 5265369600,
+                     "tflops": 4.841, "kernel_ms": 1.0877, "peak_source": "measured hbm_gbs",
+                     "traffic_GBps": 5543.6, "traffic_frac": 0.8157},
+        "gpu_launches": 40,
+        "e2e": {"value": 251.134, "unit": "GB/s", "h2d_bytes_per_step": 680542804,
+                "d2h_bytes_per_step": 512000000, "ms_per_step": 4.749, "entry_point": "spmm_eb_pr",
+                "statistic": "median of 10 calls (mean 4.749 ms)"},
+        "cpu_baseline": {"value": 5.154, "unit": "GB/s", "cores": 16, "kind": "port",
+                         "cpu_model": "Neoverse-V2",
+                         "sample": "full workload, median of 42 runs after warm-up (0.231 s "
+                                   "each, 9.7 s in all)",
+                         "one_thread": {"value": 0.397, "sample": "rows [0, 794298) (81.0% of "
+                                                                  "nonzeros), one run"},
+                         "build": "-O3 -fopenmp -mcpu=neoverse-v2"},
+        "clocks": {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "samples": 1, "interval_ms": 20,
+                   "nvml_samples": 9, "reasons": []},
+        "schedules": {s: {"kernel_ms": 1.7344, "roofline_frac": 0.1012, "max_err_vs_fp64": 2.1e-07}
+                      for s in S},
+        "power_law_10m": {"schedules": {s: {"kernel_ms": 1.0266} for s in S},
+                          "spmv": {"ms": 0.0888}},
+        "reference_gpu": {w: {"segtaco": {s: {"ms": 26.0697} for s in S},
+                              "ours": {s: {"ms": 1.1173} for s in S}, "max_err_vs_fp64": 2e-07}
+                          for w in ("power_law", "uniform16")},
+        "vendor": {"ms_per_step": 2.2488},
+        "batched": {"speedup_vs_per_call": 2.919, "per_call_graph_ms": 10.837,
+                    "per_call_ms": 11.882, "batched_graph_ms": 3.712, "max_err_vs_fp64": 1.37e-07},
+        "served": dict(served(), bf16_operands=served(), device_operands=served()),
+        "side_ops": {k: {"ms": 0.2467, "roofline_frac": 0.2176, "max_err_vs_fp64": 2.2e-07}
+                     for k in ("spmv_power_law", "spmm_power_law_bf16", "spmspv_power_law",
+                               "sddmm_banded_f32", "spmm_banded_f32", "sddmm_banded_bf16",
+                               "spmm_banded_bf16")},
+    }
+
+
+def test_result_line_fits_a_3kb_tail():
+    """The result line (printed last) keeps every contract key and, with the
+    summary, stays well inside the last 3 KB of output."""
+    import json
+    line = bench.result_line(_sample_detail())
+    assert set(bench.RESULT_KEYS) <= set(line)
+    assert "summary" in line and "schedules" in line["summary"]
+    assert "gathered_bytes" not in line["roofline"] and line["roofline"]["frac"] == 0.1613
+    assert line["cpu_baseline"]["one_thread"] == {"value": 0.397}
+    assert line["clocks"] == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": []}
+    assert len(json.dumps(line, separators=(",", ":"))) < 2750
